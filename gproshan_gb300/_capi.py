@@ -1,0 +1,308 @@
+"""ctypes binding of libgp_ptp.so (the C ABI declared in include/gp_ptp.h).
+
+The library is built in-tree by ``gproshan_gb300.build``.  There is no
+fallback: if the shared library is missing or no GB300 is visible, every
+call raises.
+"""
+from __future__ import annotations
+
+import atexit
+import ctypes as C
+import os
+import threading
+import weakref
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libgp_ptp.so")
+
+GP_OK = 0
+GP_F32 = 0
+GP_F64 = 1
+GP_BATCH_DEVICE_POINTERS = 1
+NIL = 0xFFFFFFFF
+
+STATUS = {
+    0: "GP_OK", 1: "GP_ERR_INVALID_ARG", 2: "GP_ERR_NONMANIFOLD", 3: "GP_ERR_NO_CONVERGENCE",
+    4: "GP_ERR_DEVICE_TIMEOUT", 5: "GP_ERR_CUDA", 6: "GP_ERR_NO_DEVICE", 7: "GP_ERR_OUT_OF_MEMORY",
+    8: "GP_ERR_CAPACITY",
+}
+
+
+class GPError(RuntimeError):
+    """A libgp_ptp call returned a status other than GP_OK."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+
+
+class gp_ptp_opts(C.Structure):
+    _fields_ = [("precision", C.c_uint32), ("max_iter", C.c_uint32), ("tol", C.c_double),
+                ("threads", C.c_uint32), ("ctas", C.c_uint32), ("local_window", C.c_uint32),
+                ("reserved", C.c_uint32 * 3)]
+
+
+class gp_ptp_stats(C.Structure):
+    _fields_ = [("n_iter", C.c_uint32), ("n_limits", C.c_uint32), ("relaxations", C.c_uint64),
+                ("seconds", C.c_double)]
+
+
+class gp_field(C.Structure):
+    _fields_ = [("mesh", C.c_void_p), ("sources", C.c_void_p), ("n_sources", C.c_uint32),
+                ("dist", C.c_void_p), ("clusters", C.c_void_p), ("stats", C.c_void_p)]
+
+
+# every symbol declared in include/gp_ptp.h, with (restype, argtypes)
+_u32p = C.POINTER(C.c_uint32)
+SIGNATURES = {
+    "gp_ctx_create": (C.c_int, [C.c_int, C.POINTER(C.c_void_p)]),
+    "gp_ctx_destroy": (None, [C.c_void_p]),
+    "gp_ctx_last_error": (C.c_char_p, [C.c_void_p]),
+    "gp_status_str": (C.c_char_p, [C.c_int]),
+    "gp_ctx_stream": (C.c_void_p, [C.c_void_p]),
+    "gp_ctx_workspace_bytes": (C.c_size_t, [C.c_void_p]),
+    "gp_che_build": (C.c_int, [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                               C.POINTER(C.c_int)]),
+    "gp_mesh_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+                                 C.c_void_p, C.POINTER(C.c_void_p)]),
+    "gp_mesh_destroy": (None, [C.c_void_p]),
+    "gp_mesh_n_vertices": (C.c_uint32, [C.c_void_p]),
+    "gp_mesh_n_faces": (C.c_uint32, [C.c_void_p]),
+    "gp_toplesets": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+                               C.c_uint32, C.c_void_p, C.c_uint32, _u32p]),
+    "gp_ptp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                         C.c_void_p, C.POINTER(gp_ptp_opts), C.c_void_p, C.c_int, C.c_void_p,
+                         C.POINTER(gp_ptp_stats)]),
+    "gp_ptp_batch": (C.c_int, [C.c_void_p, C.POINTER(gp_field), C.c_uint32, C.POINTER(gp_ptp_opts),
+                               C.c_int, C.c_uint32, C.POINTER(C.c_double)]),
+    "gp_normalize_ptp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64]),
+    "gp_fps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64,
+                         C.c_double, C.POINTER(gp_ptp_opts), _u32p, C.POINTER(C.c_double),
+                         C.POINTER(C.c_double)]),
+}
+
+_lib = None
+_lock = threading.Lock()
+_live_meshes = weakref.WeakSet()
+_live_contexts = weakref.WeakSet()
+
+
+@atexit.register
+def _release_all():
+    # free device meshes, then contexts, while the CUDA runtime is still up
+    for m in list(_live_meshes):
+        m.close()
+    for c in list(_live_contexts):
+        c.close()
+
+
+def lib():
+    """Load libgp_ptp.so (raises if it was not built)."""
+    global _lib
+    with _lock:
+        if _lib is None:
+            if not os.path.exists(LIB_PATH):
+                raise ImportError(f"{LIB_PATH} is missing: build it with gproshan_gb300.build.build()")
+            L = C.CDLL(LIB_PATH)
+            for name, (res, args) in SIGNATURES.items():
+                fn = getattr(L, name)
+                fn.restype = res
+                fn.argtypes = args
+            _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _u32(a):
+    return np.ascontiguousarray(a, dtype=np.uint32)
+
+
+def che_build(n_vertices: int, tri):
+    """(OT, EVT, manifold) of a triangle list (host only, no GPU needed)."""
+    VT = _u32(tri).reshape(-1)
+    nf = len(VT) // 3
+    OT = np.empty(3 * nf, np.uint32)
+    EVT = np.empty(n_vertices, np.uint32)
+    man = C.c_int(0)
+    st = lib().gp_che_build(n_vertices, nf, _ptr(VT), _ptr(OT), _ptr(EVT), C.byref(man))
+    if st != GP_OK:
+        raise GPError(st, "gp_che_build: triangle index out of range")
+    return OT, EVT, bool(man.value)
+
+
+class Context:
+    """A gp_ctx: one CUDA stream and a reusable device workspace."""
+
+    def __init__(self, device: int = 0):
+        self._h = C.c_void_p()
+        st = lib().gp_ctx_create(device, C.byref(self._h))
+        if st != GP_OK:
+            raise GPError(st, f"gp_ctx_create(device={device}) failed")
+        self.device = device
+        _live_contexts.add(self)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def check(self, st: int, what: str):
+        if st != GP_OK:
+            raise GPError(st, f"{what}: {lib().gp_ctx_last_error(self._h).decode()}")
+
+    def workspace_bytes(self) -> int:
+        return int(lib().gp_ctx_workspace_bytes(self._h))
+
+    def close(self):
+        if self._h:
+            lib().gp_ctx_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+_default = {}
+
+
+def default_context(device: int = 0) -> Context:
+    if device not in _default:
+        _default[device] = Context(device)
+    return _default[device]
+
+
+class DeviceMesh:
+    """A gp_mesh: CHE tables uploaded once, star lists built on the device."""
+
+    def __init__(self, ctx: Context, xyz, VT, OT=None, EVT=None):
+        self.ctx = ctx
+        xyz = np.ascontiguousarray(xyz, dtype=np.float64).reshape(-1, 3)
+        VT = _u32(VT).reshape(-1)
+        self.n_vertices = len(xyz)
+        self.n_faces = len(VT) // 3
+        self._h = C.c_void_p()
+        st = lib().gp_mesh_create(ctx.handle, self.n_vertices, _ptr(xyz), self.n_faces, _ptr(VT),
+                                  _ptr(None if OT is None else _u32(OT)),
+                                  _ptr(None if EVT is None else _u32(EVT)), C.byref(self._h))
+        ctx.check(st, "gp_mesh_create")
+        _live_meshes.add(self)
+
+    @property
+    def handle(self):
+        return self._h
+
+    def close(self):
+        if self._h:
+            lib().gp_mesh_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def toplesets(mesh: DeviceMesh, sources):
+    """(rings, sorted, limits) computed on the GPU (gp_toplesets)."""
+    src = _u32(sources)
+    nv = mesh.n_vertices
+    rings = np.empty(nv, np.uint32)
+    srt = np.empty(nv + len(src), np.uint32)
+    lim = np.empty(nv + 2, np.uint32)
+    nl = C.c_uint32(0)
+    st = lib().gp_toplesets(mesh.ctx.handle, mesh.handle, _ptr(src), len(src), _ptr(rings), _ptr(srt),
+                            len(srt), _ptr(lim), len(lim), C.byref(nl))
+    mesh.ctx.check(st, "gp_toplesets")
+    lim = lim[:nl.value].copy()
+    return rings, srt[:lim[-1]].copy() if len(lim) else srt[:0].copy(), lim
+
+
+def make_opts(precision: int = GP_F32, max_iter: int = 0, tol: float = 0.0, ctas: int = 0,
+              local_window: int = 0) -> gp_ptp_opts:
+    o = gp_ptp_opts()
+    o.precision = precision
+    o.max_iter = max_iter
+    o.tol = tol
+    o.ctas = ctas
+    o.local_window = local_window
+    return o
+
+
+def ptp(mesh: DeviceMesh, sources, limits=None, sorted_=None, dtype=np.float32, precision=None,
+        clusters=None, opts: gp_ptp_opts | None = None):
+    """Distances (and labels if ``clusters`` is an initial label array) on the GPU.
+    Returns (dist, clusters_or_None, stats)."""
+    src = _u32(sources)
+    out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
+    if opts is None:
+        opts = make_opts(GP_F32 if precision is None else precision)
+    elif precision is not None:
+        opts.precision = precision
+    dist = np.empty(mesh.n_vertices, dtype=np.float64 if out_t == GP_F64 else np.float32)
+    cl = None if clusters is None else _u32(clusters).copy()
+    lim = None if limits is None else _u32(limits)
+    srt = None if sorted_ is None else _u32(sorted_)
+    stats = gp_ptp_stats()
+    st = lib().gp_ptp(mesh.ctx.handle, mesh.handle, _ptr(src), len(src), _ptr(lim),
+                      0 if lim is None else len(lim), _ptr(srt), C.byref(opts), _ptr(dist), out_t, _ptr(cl),
+                      C.byref(stats))
+    mesh.ctx.check(st, "gp_ptp")
+    return dist, cl, stats
+
+
+def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP_F32, ctas: int = 0,
+              with_stats: bool = True, local_window: int = 0):
+    """Solve many fields together (host arrays).  Returns (dists, stats, seconds)."""
+    n = len(sources_list)
+    out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
+    fields = (gp_field * n)()
+    keep = []
+    dists = []
+    stats = [gp_ptp_stats() for _ in range(n)]
+    for k in range(n):
+        src = _u32(sources_list[k])
+        d = np.empty(meshes[k].n_vertices, dtype=np.float64 if out_t == GP_F64 else np.float32)
+        keep.append(src)
+        dists.append(d)
+        fields[k].mesh = meshes[k].handle
+        fields[k].sources = src.ctypes.data
+        fields[k].n_sources = len(src)
+        fields[k].dist = d.ctypes.data
+        fields[k].clusters = None
+        fields[k].stats = C.addressof(stats[k]) if with_stats else None
+    sec = C.c_double(0)
+    opts = make_opts(precision, ctas=ctas, local_window=local_window)
+    st = lib().gp_ptp_batch(ctx.handle, fields, n, C.byref(opts), out_t, 0, C.byref(sec))
+    ctx.check(st, "gp_ptp_batch")
+    return dists, stats, sec.value
+
+
+def normalize_ptp(ctx: Context, dist):
+    d = np.ascontiguousarray(dist)
+    t = GP_F64 if d.dtype == np.float64 else GP_F32
+    st = lib().gp_normalize_ptp(ctx.handle, _ptr(d), t, len(d))
+    ctx.check(st, "gp_normalize_ptp")
+    return d
+
+
+def fps(mesh: DeviceMesh, n: int, seeds=(0,), radio: float = 0.0, precision=GP_F32):
+    """farthest_point_sampling_ptp_gpu: (samples, max_dist, seconds)."""
+    cap = max(int(n), len(seeds)) + 1
+    s = np.zeros(cap, np.uint32)
+    s[:len(seeds)] = seeds
+    n_out = C.c_uint32(0)
+    md = C.c_double(0)
+    sec = C.c_double(0)
+    opts = make_opts(precision)
+    st = lib().gp_fps(mesh.ctx.handle, mesh.handle, _ptr(s), len(seeds), cap, int(n), float(radio),
+                      C.byref(opts), C.byref(n_out), C.byref(md), C.byref(sec))
+    mesh.ctx.check(st, "gp_fps")
+    return s[:n_out.value].copy(), md.value, sec.value

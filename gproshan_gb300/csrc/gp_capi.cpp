@@ -1,0 +1,840 @@
+// C ABI of libgp_ptp.so (include/gp_ptp.h): argument checks, device workspace,
+// per-call layout of the field buffers, and the launch sequence
+//   toplesets (BFS) -> ring renumbering -> persistent sweeps -> gather.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "gp_internal.h"
+
+namespace gp {
+// launchers defined in the .cu files and not in gp_internal.h's first list
+cudaError_t launch_fan_fill(const uint32_t *VT, const uint32_t *OT, const uint32_t *EVT, uint32_t nv,
+                            const uint32_t *flags, uint32_t *off, uint32_t *fan, cudaStream_t s);
+cudaError_t launch_strip_flags(const uint32_t *in, uint32_t *out, uint32_t n, cudaStream_t s);
+cudaError_t launch_bfs_setup(FieldDev *fields, FieldState *state, const uint32_t *vbase, uint32_t n_fields,
+                             uint32_t total_vertices, cudaStream_t s);
+cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
+                                  uint32_t total, uint32_t *cnt, uint32_t *scan_tmp, bool f64, bool clusters,
+                                  cudaStream_t s);
+cudaError_t launch_gather_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
+                                uint32_t total, bool f64, bool clusters, cudaStream_t s);
+cudaError_t launch_normalize(void *dist, bool f64, uint64_t n, unsigned long long *tmp, cudaStream_t s);
+int ptp_threads();
+int ptp_local_max_ctas(int device, bool f64, bool clusters);
+cudaError_t launch_classify(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
+                            cudaStream_t s);
+cudaError_t launch_ptp_local(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
+                             uint32_t ctas, bool f64, bool clusters, cudaStream_t s);
+} // namespace gp
+
+using namespace gp;
+
+struct gp_ctx {
+	int device = 0;
+	cudaStream_t stream = nullptr;
+	int num_sms = 0;
+	std::string err;
+	void *ws = nullptr;        // grow-only device workspace
+	size_t ws_bytes = 0;
+	void *pin = nullptr;       // grow-only pinned host staging
+	size_t pin_bytes = 0;
+	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	int bfs_ctas = 0;
+	int ptp_ctas[4] = {0, 0, 0, 0};
+	int local_ctas[4] = {0, 0, 0, 0};
+};
+
+struct gp_mesh {
+	gp_ctx *ctx = nullptr;
+	uint32_t nv = 0, nf = 0;
+	MeshDev dev{};
+	void *block = nullptr;     // one device allocation holding the mesh arrays
+};
+
+namespace {
+
+void set_err(gp_ctx *ctx, const char *fmt, ...)
+{
+	if(!ctx) return;
+	char buf[512];
+	va_list ap;
+	va_start(ap, fmt);
+	vsnprintf(buf, sizeof(buf), fmt, ap);
+	va_end(ap);
+	ctx->err = buf;
+}
+
+#define GP_CUDA(ctx, call)                                                                     \
+	do {                                                                                       \
+		cudaError_t e_ = (call);                                                               \
+		if(e_ != cudaSuccess)                                                                  \
+		{                                                                                      \
+			set_err(ctx, "%s: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+			return e_ == cudaErrorMemoryAllocation ? GP_ERR_OUT_OF_MEMORY : GP_ERR_CUDA;        \
+		}                                                                                      \
+	} while(0)
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Offsets of the buffers of one call inside the workspace.
+struct Carve {
+	size_t off = 0;
+	template <class T> size_t add(size_t n)
+	{
+		off = align_up(off, 256);
+		const size_t o = off;
+		off += std::max<size_t>(n, 1) * sizeof(T);
+		return o;
+	}
+};
+
+gp_status ensure_ws(gp_ctx *ctx, size_t bytes)
+{
+	if(bytes <= ctx->ws_bytes) return GP_OK;
+	if(ctx->ws)
+	{
+		GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+		GP_CUDA(ctx, cudaFree(ctx->ws));
+		ctx->ws = nullptr;
+		ctx->ws_bytes = 0;
+	}
+	const size_t want = align_up(bytes + bytes / 8, 1 << 20);
+	GP_CUDA(ctx, cudaMalloc(&ctx->ws, want));
+	ctx->ws_bytes = want;
+	return GP_OK;
+}
+
+gp_status ensure_pin(gp_ctx *ctx, size_t bytes)
+{
+	if(bytes <= ctx->pin_bytes) return GP_OK;
+	if(ctx->pin)
+	{
+		GP_CUDA(ctx, cudaStreamSynchronize(ctx->stream));
+		GP_CUDA(ctx, cudaFreeHost(ctx->pin));
+		ctx->pin = nullptr;
+		ctx->pin_bytes = 0;
+	}
+	const size_t want = align_up(bytes + bytes / 8, 1 << 16);
+	GP_CUDA(ctx, cudaMallocHost(&ctx->pin, want));
+	ctx->pin_bytes = want;
+	return GP_OK;
+}
+
+bool is_device_ptr(const void *p)
+{
+	cudaPointerAttributes a;
+	if(cudaPointerGetAttributes(&a, p) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return false;
+	}
+	return a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged;
+}
+
+// One field request of a call.
+struct Req {
+	gp_mesh *mesh;
+	const uint32_t *src;
+	uint32_t ns;
+	const uint32_t *limits;   // host toplesets or null
+	uint32_t nl;
+	const uint32_t *sorted;
+	void *dist;               // output (host or device)
+	uint32_t *clusters;       // in/out labels or null
+	gp_ptp_stats *stats;
+};
+
+enum class Stage { toplesets, ptp };
+
+struct TopOut {  // host outputs of gp_toplesets
+	uint32_t *rings;
+	uint32_t *sorted;
+	uint32_t cap_sorted;
+	uint32_t *limits;
+	uint32_t cap_limits;
+	uint32_t *n_limits;
+};
+
+gp_status map_dev_err(gp_ctx *ctx, uint32_t err, const char *where)
+{
+	if(!err) return GP_OK;
+	if(err & DEV_ERR_TIMEOUT)
+	{
+		set_err(ctx, "%s: a device-side barrier wait ran past its limit", where);
+		return GP_ERR_DEVICE_TIMEOUT;
+	}
+	set_err(ctx, "%s: device reported an index outside its buffer (err=%u)", where, err);
+	return GP_ERR_INVALID_ARG;
+}
+
+gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts, gp_dtype out_type,
+              bool src_dev, bool out_dev, Stage stage, const TopOut *top, double *seconds)
+{
+	if(!ctx) return GP_ERR_INVALID_ARG;
+	if(!F) return GP_OK;
+	const gp_ptp_opts o = opts ? *opts : gp_ptp_opts{};
+	const bool f64 = o.precision == GP_F64;
+	const bool clusters = stage == Stage::ptp && std::any_of(reqs, reqs + F, [](const Req &r) { return r.clusters; });
+	const bool given_tops = reqs[0].limits != nullptr;
+	const size_t tsz = f64 ? sizeof(double) : sizeof(float);
+	const size_t osz = out_type == GP_F64 ? sizeof(double) : sizeof(float);
+	const uint32_t NTH = (uint32_t) ptp_threads();
+
+	// ---- checks and layout -------------------------------------------------
+	std::vector<uint32_t> base(F + 1), vbase(F + 1), fbase(F + 1), sbase(F + 1);
+	uint64_t tot = 0, vtot = 0, ftot = 0, stot = 0, tiles = 0;
+	for(uint32_t f = 0; f < F; f++)
+	{
+		const Req &r = reqs[f];
+		if(!r.mesh || r.mesh->ctx != ctx || !r.src || !r.ns)
+		{
+			set_err(ctx, "field %u: null mesh/sources, empty source list, or mesh of another context", f);
+			return GP_ERR_INVALID_ARG;
+		}
+		if(stage == Stage::ptp && !r.dist)
+		{
+			set_err(ctx, "field %u: null dist", f);
+			return GP_ERR_INVALID_ARG;
+		}
+		if(given_tops != (r.limits != nullptr) || (r.limits && (!r.sorted || r.nl < 1 || F != 1)))
+		{
+			set_err(ctx, "toplesets must be given for a single field with both limits and sorted");
+			return GP_ERR_INVALID_ARG;
+		}
+		const uint32_t nv = r.mesh->nv;
+		if(!src_dev)
+			for(uint32_t s = 0; s < r.ns; s++)
+				if(r.src[s] >= nv)
+				{
+					set_err(ctx, "field %u: source %u = %u out of range (n_vertices %u)", f, s, r.src[s], nv);
+					return GP_ERR_INVALID_ARG;
+				}
+		base[f] = (uint32_t) tot;
+		vbase[f] = (uint32_t) vtot;
+		fbase[f] = (uint32_t) ftot;
+		sbase[f] = (uint32_t) stot;
+		const uint64_t S = (uint64_t) nv + r.ns + 2;
+		tot += S;
+		vtot += nv;
+		ftot += (uint64_t) r.mesh->dev.n_fan + (uint64_t) r.ns * r.mesh->dev.max_fan;
+		stot += r.ns;
+		tiles += (S + NTH - 1) / NTH + 1;
+	}
+	base[F] = (uint32_t) tot;
+	vbase[F] = (uint32_t) vtot;
+	fbase[F] = (uint32_t) ftot;
+	sbase[F] = (uint32_t) stot;
+	if(tot >= (1ull << 31) || ftot >= (1ull << 31))
+	{
+		set_err(ctx, "batch too large (%llu slots, %llu fan entries): split it", (unsigned long long) tot,
+		        (unsigned long long) ftot);
+		return GP_ERR_CAPACITY;
+	}
+	if(given_tops)
+	{
+		const Req &r = reqs[0];
+		const uint32_t cap = r.mesh->nv + r.ns;
+		if(r.nl > r.mesh->nv + 2 || r.limits[r.nl - 1] > cap || r.limits[0] != 0)
+		{
+			set_err(ctx, "toplesets limits out of range");
+			return GP_ERR_INVALID_ARG;
+		}
+		for(uint32_t k = 1; k < r.nl; k++)
+			if(r.limits[k] < r.limits[k - 1])
+			{
+				set_err(ctx, "toplesets limits not increasing at %u", k);
+				return GP_ERR_INVALID_ARG;
+			}
+		for(uint32_t k = 0; k < r.limits[r.nl - 1]; k++)
+			if(r.sorted[k] >= r.mesh->nv)
+			{
+				set_err(ctx, "toplesets sorted[%u] out of range", k);
+				return GP_ERR_INVALID_ARG;
+			}
+	}
+
+	Carve cv;
+	const size_t o_fields = cv.add<FieldDev>(F), o_state = cv.add<FieldState>(F), o_plan = cv.add<PlanDev>(1);
+	const size_t o_act = cv.add<uint32_t>(F), o_ts = cv.add<uint32_t>(F + 1), o_aux = cv.add<uint32_t>(tiles + 2);
+	const size_t o_sync = cv.add<GridSync>(2), o_base = cv.add<uint32_t>(F + 1), o_vbase = cv.add<uint32_t>(F + 1);
+	const size_t o_queue = cv.add<uint32_t>(4);
+	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
+	const size_t o_sorted = cv.add<uint32_t>(tot), o_lim = cv.add<uint32_t>(tot), o_inv = cv.add<uint32_t>(tot);
+	size_t o_cnt = 0, o_scan = 0, o_P = 0, o_Pd = 0, o_off = 0, o_fan = 0, o_D0 = 0, o_D1 = 0, o_C0 = 0, o_C1 = 0;
+	size_t o_out = 0, o_cout = 0, o_cin = 0;
+	if(stage == Stage::ptp)
+	{
+		o_cnt = cv.add<uint32_t>(tot + 1);
+		o_scan = cv.add<uint32_t>(scan_tmp_words(tot));
+		o_P = cv.add<float4>(tot);
+		if(f64) o_Pd = cv.add<double>(4 * tot);
+		o_off = cv.add<uint32_t>(tot);
+		o_fan = cv.add<uint32_t>(ftot);
+		o_D0 = cv.add<char>(tot * tsz);
+		o_D1 = cv.add<char>(tot * tsz);
+		if(clusters)
+		{
+			o_C0 = cv.add<uint32_t>(tot);
+			o_C1 = cv.add<uint32_t>(tot);
+			o_cout = cv.add<uint32_t>(vtot);
+			o_cin = cv.add<uint32_t>(vtot);
+		}
+		if(!out_dev) o_out = cv.add<char>(vtot * osz);
+	}
+	const size_t o_src = cv.add<uint32_t>(stot);
+	gp_status st = ensure_ws(ctx, cv.off);
+	if(st != GP_OK) return st;
+	char *W = static_cast<char *>(ctx->ws);
+	auto P = [&](size_t off) { return W + off; };
+
+	// ---- host-side descriptors -------------------------------------------------
+	std::vector<FieldDev> hf(F);
+	std::vector<FieldState> hs(F);
+	std::memset(hs.data(), 0, sizeof(FieldState) * F);
+	for(uint32_t f = 0; f < F; f++)
+	{
+		const Req &r = reqs[f];
+		FieldDev &d = hf[f];
+		std::memset(&d, 0, sizeof(d));
+		d.m = r.mesh->dev;
+		d.ns = r.ns;
+		d.cap_sorted = r.mesh->nv + r.ns;
+		d.src = src_dev ? r.src : reinterpret_cast<const uint32_t *>(P(o_src)) + sbase[f];
+		d.ring = reinterpret_cast<uint32_t *>(P(o_ring)) + base[f];
+		d.key = reinterpret_cast<unsigned long long *>(P(o_key)) + base[f];
+		d.sorted = reinterpret_cast<uint32_t *>(P(o_sorted)) + base[f];
+		d.limits = reinterpret_cast<uint32_t *>(P(o_lim)) + base[f];
+		d.inv = reinterpret_cast<uint32_t *>(P(o_inv)) + base[f];
+		if(stage == Stage::ptp)
+		{
+			d.P = reinterpret_cast<float4 *>(P(o_P)) + base[f];
+			d.Pd = f64 ? reinterpret_cast<double *>(P(o_Pd)) + 4ull * base[f] : nullptr;
+			d.off = reinterpret_cast<uint32_t *>(P(o_off)) + base[f];
+			d.fan = reinterpret_cast<uint32_t *>(P(o_fan));
+			d.D[0] = P(o_D0) + (size_t) base[f] * tsz;
+			d.D[1] = P(o_D1) + (size_t) base[f] * tsz;
+			if(clusters)
+			{
+				d.C[0] = reinterpret_cast<uint32_t *>(P(o_C0)) + base[f];
+				d.C[1] = reinterpret_cast<uint32_t *>(P(o_C1)) + base[f];
+				if(r.clusters)
+				{
+					d.clusters_out = out_dev ? r.clusters : reinterpret_cast<uint32_t *>(P(o_cout)) + vbase[f];
+					d.clusters_in = out_dev ? r.clusters : reinterpret_cast<uint32_t *>(P(o_cin)) + vbase[f];
+				}
+			}
+			d.dist_out = out_dev ? r.dist : P(o_out) + (size_t) vbase[f] * osz;
+			d.out_f64 = out_type == GP_F64;
+			d.max_iter = o.max_iter;
+			d.tol = o.tol > 0 ? o.tol : GP_PTP_TOL;
+		}
+		if(given_tops) hs[f].n_limits = r.nl;
+	}
+	// in-place label input and output on device pointers would race; stage them
+	if(clusters && out_dev)
+		for(uint32_t f = 0; f < F; f++)
+			if(reqs[f].clusters)
+				hf[f].clusters_in = reinterpret_cast<uint32_t *>(P(o_cin)) + vbase[f];
+
+	// ---- uploads -------------------------------------------------------------
+	cudaStream_t s = ctx->stream;
+	size_t pin_need = sizeof(FieldDev) * F + sizeof(FieldState) * F + 8 * (F + 1) + 4 * (size_t) stot + 64;
+	if(given_tops) pin_need += 4 * ((size_t) reqs[0].nl + reqs[0].limits[reqs[0].nl - 1]) + 64;
+	st = ensure_pin(ctx, pin_need);
+	if(st != GP_OK) return st;
+	GP_CUDA(ctx, cudaStreamSynchronize(s));  // the staging buffer may still feed a previous call
+	char *pin = static_cast<char *>(ctx->pin);
+	size_t po = 0;
+	auto stage_copy = [&](size_t dst_off, const void *src, size_t bytes) -> cudaError_t {
+		std::memcpy(pin + po, src, bytes);
+		cudaError_t e = cudaMemcpyAsync(P(dst_off), pin + po, bytes, cudaMemcpyHostToDevice, s);
+		po = align_up(po + bytes, 16);
+		return e;
+	};
+	GP_CUDA(ctx, stage_copy(o_fields, hf.data(), sizeof(FieldDev) * F));
+	GP_CUDA(ctx, stage_copy(o_state, hs.data(), sizeof(FieldState) * F));
+	GP_CUDA(ctx, stage_copy(o_base, base.data(), 4 * (F + 1)));
+	GP_CUDA(ctx, stage_copy(o_vbase, vbase.data(), 4 * (F + 1)));
+	if(!src_dev)
+	{
+		std::vector<uint32_t> all(stot);
+		for(uint32_t f = 0; f < F; f++) std::memcpy(all.data() + sbase[f], reqs[f].src, 4 * (size_t) reqs[f].ns);
+		GP_CUDA(ctx, stage_copy(o_src, all.data(), 4 * stot));
+	}
+	if(given_tops)
+	{
+		const Req &r = reqs[0];
+		GP_CUDA(ctx, stage_copy(o_lim, r.limits, 4 * (size_t) r.nl));
+		GP_CUDA(ctx, stage_copy(o_sorted, r.sorted, 4 * (size_t) r.limits[r.nl - 1]));
+	}
+	if(clusters)
+		for(uint32_t f = 0; f < F; f++)
+			if(reqs[f].clusters)
+			{
+				const size_t bytes = 4 * (size_t) reqs[f].mesh->nv;
+				uint32_t *dst = reinterpret_cast<uint32_t *>(P(o_cin)) + vbase[f];
+				GP_CUDA(ctx, cudaMemcpyAsync(dst, reqs[f].clusters, bytes,
+				                             out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+			}
+	PlanDev hp{};
+	hp.act = reinterpret_cast<uint32_t *>(P(o_act));
+	hp.tile_start = reinterpret_cast<uint32_t *>(P(o_ts));
+	hp.tile_aux = reinterpret_cast<uint32_t *>(P(o_aux));
+	hp.cap_tiles = (uint32_t) tiles;
+	GP_CUDA(ctx, cudaMemcpyAsync(P(o_plan), &hp, sizeof(hp), cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));  // hp lives on this stack frame
+
+	FieldDev *dF = reinterpret_cast<FieldDev *>(P(o_fields));
+	FieldState *dS = reinterpret_cast<FieldState *>(P(o_state));
+	PlanDev *dP = reinterpret_cast<PlanDev *>(P(o_plan));
+	GridSync *dSync = reinterpret_cast<GridSync *>(P(o_sync));
+	const uint32_t *dBase = reinterpret_cast<const uint32_t *>(P(o_base));
+	const uint32_t *dVbase = reinterpret_cast<const uint32_t *>(P(o_vbase));
+
+	// ---- device work ---------------------------------------------------------
+	GP_CUDA(ctx, cudaMemsetAsync(dSync, 0, 2 * sizeof(GridSync), s));
+	GP_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+	if(!given_tops)
+	{
+		GP_CUDA(ctx, launch_bfs_setup(dF, dS, dVbase, F, (uint32_t) vtot, s));
+		GP_CUDA(ctx, launch_toplesets(dF, dS, F, &dSync->count, (uint32_t) ctx->bfs_ctas, s));
+	}
+	if(stage == Stage::ptp)
+	{
+		GP_CUDA(ctx, launch_renumber_batch(dF, dS, dBase, F, (uint32_t) tot, reinterpret_cast<uint32_t *>(P(o_cnt)),
+		                                   reinterpret_cast<uint32_t *>(P(o_scan)), f64, clusters, s));
+		const int kv = (f64 ? 2 : 0) + (clusters ? 1 : 0);
+		const uint32_t lw = o.local_window ? o.local_window : 4096u;
+		GP_CUDA(ctx, launch_classify(dF, dS, F, lw, s));
+		GP_CUDA(ctx, launch_ptp_local(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_queue)),
+		                              (uint32_t) ctx->local_ctas[kv], f64, clusters, s));
+		const int maxc = ctx->ptp_ctas[kv];
+		uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
+		GP_CUDA(ctx, launch_ptp(dF, dS, F, dP, dSync + 1, ctas, f64, clusters, s));
+		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s));
+	}
+	GP_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+
+	// ---- downloads -------------------------------------------------------------
+	GridSync hsync[2];
+	GP_CUDA(ctx, cudaMemcpyAsync(hsync, dSync, sizeof(hsync), cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(hs.data(), dS, sizeof(FieldState) * F, cudaMemcpyDeviceToHost, s));
+	if(stage == Stage::ptp && !out_dev)
+		for(uint32_t f = 0; f < F; f++)
+		{
+			const size_t nv = reqs[f].mesh->nv;
+			GP_CUDA(ctx, cudaMemcpyAsync(reqs[f].dist, P(o_out) + (size_t) vbase[f] * osz, nv * osz,
+			                             cudaMemcpyDeviceToHost, s));
+			if(reqs[f].clusters)
+				GP_CUDA(ctx, cudaMemcpyAsync(reqs[f].clusters, reinterpret_cast<uint32_t *>(P(o_cout)) + vbase[f],
+				                             4 * nv, cudaMemcpyDeviceToHost, s));
+		}
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
+	uint32_t ferr = 0;
+	for(uint32_t f = 0; f < F; f++) ferr |= hs[f].status;
+	st = map_dev_err(ctx, hsync[0].err | hsync[1].err | ferr, stage == Stage::ptp ? "ptp" : "toplesets");
+	if(st != GP_OK) return st;
+	float ms = 0.f;
+	GP_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+	if(seconds) *seconds = ms * 1e-3;
+	for(uint32_t f = 0; f < F; f++)
+		if(reqs[f].stats)
+		{
+			reqs[f].stats->n_iter = hs[f].n_iter;
+			reqs[f].stats->n_limits = hs[f].n_limits;
+			reqs[f].stats->relaxations = hs[f].relax;
+			reqs[f].stats->seconds = ms * 1e-3;
+		}
+
+	if(stage == Stage::toplesets && top)
+	{
+		const Req &r = reqs[0];
+		const uint32_t nl = hs[0].n_limits;
+		if(top->n_limits) *top->n_limits = nl;
+		std::vector<uint32_t> lim(nl);
+		if(nl) GP_CUDA(ctx, cudaMemcpy(lim.data(), P(o_lim), 4 * (size_t) nl, cudaMemcpyDeviceToHost));
+		const uint32_t nr = nl ? lim[nl - 1] : 0;
+		if(top->rings)
+			GP_CUDA(ctx, cudaMemcpy(top->rings, P(o_ring), 4 * (size_t) r.mesh->nv, cudaMemcpyDeviceToHost));
+		if(nl > top->cap_limits || nr > top->cap_sorted)
+		{
+			set_err(ctx, "toplesets: need %u limits and %u sorted entries", nl, nr);
+			return GP_ERR_CAPACITY;
+		}
+		if(top->limits && nl) std::memcpy(top->limits, lim.data(), 4 * (size_t) nl);
+		if(top->sorted && nr) GP_CUDA(ctx, cudaMemcpy(top->sorted, P(o_sorted), 4 * (size_t) nr, cudaMemcpyDeviceToHost));
+	}
+	return GP_OK;
+}
+
+} // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char *gp_status_str(gp_status s)
+{
+	switch(s)
+	{
+		case GP_OK: return "ok";
+		case GP_ERR_INVALID_ARG: return "invalid argument";
+		case GP_ERR_NONMANIFOLD: return "star walk does not close";
+		case GP_ERR_NO_CONVERGENCE: return "no convergence";
+		case GP_ERR_DEVICE_TIMEOUT: return "device wait timed out";
+		case GP_ERR_CUDA: return "CUDA error";
+		case GP_ERR_NO_DEVICE: return "no usable CUDA device";
+		case GP_ERR_OUT_OF_MEMORY: return "out of memory";
+		case GP_ERR_CAPACITY: return "buffer too small";
+	}
+	return "unknown status";
+}
+
+gp_status gp_ctx_create(int device, gp_ctx **out)
+{
+	if(!out) return GP_ERR_INVALID_ARG;
+	*out = nullptr;
+	int n = 0;
+	if(cudaGetDeviceCount(&n) != cudaSuccess || device < 0 || device >= n)
+	{
+		cudaGetLastError();
+		return GP_ERR_NO_DEVICE;
+	}
+	int major = 0, minor = 0;
+	cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, device);
+	cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, device);
+	if(major != 10 || minor != 3) return GP_ERR_NO_DEVICE;  // built for sm_103a only
+	gp_ctx *ctx = new gp_ctx;
+	ctx->device = device;
+	if(cudaSetDevice(device) != cudaSuccess || cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+	   cudaEventCreate(&ctx->ev0) != cudaSuccess || cudaEventCreate(&ctx->ev1) != cudaSuccess)
+	{
+		cudaGetLastError();
+		delete ctx;
+		return GP_ERR_CUDA;
+	}
+	cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+	ctx->bfs_ctas = toplesets_max_ctas(device);
+	for(int k = 0; k < 4; k++)
+	{
+		ctx->ptp_ctas[k] = ptp_max_ctas(device, k >= 2, k & 1);
+		ctx->local_ctas[k] = ptp_local_max_ctas(device, k >= 2, k & 1);
+	}
+	if(ctx->bfs_ctas <= 0 || ctx->ptp_ctas[0] <= 0)
+	{
+		cudaGetLastError();
+		gp_ctx_destroy(ctx);
+		return GP_ERR_NO_DEVICE;
+	}
+	*out = ctx;
+	return GP_OK;
+}
+
+void gp_ctx_destroy(gp_ctx *ctx)
+{
+	if(!ctx) return;
+	cudaSetDevice(ctx->device);
+	if(ctx->stream) cudaStreamSynchronize(ctx->stream);
+	if(ctx->ws) cudaFree(ctx->ws);
+	if(ctx->pin) cudaFreeHost(ctx->pin);
+	if(ctx->ev0) cudaEventDestroy(ctx->ev0);
+	if(ctx->ev1) cudaEventDestroy(ctx->ev1);
+	if(ctx->stream) cudaStreamDestroy(ctx->stream);
+	delete ctx;
+}
+
+const char *gp_ctx_last_error(const gp_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+void *gp_ctx_stream(gp_ctx *ctx) { return ctx ? (void *) ctx->stream : nullptr; }
+size_t gp_ctx_workspace_bytes(const gp_ctx *ctx) { return ctx ? ctx->ws_bytes : 0; }
+
+gp_status gp_che_build(uint32_t nv, uint32_t nf, const uint32_t *VT, uint32_t *OT, uint32_t *EVT, int *manifold)
+{
+	// Compact half-edge opposite/extra-vertex tables with the matching order
+	// and non-manifold rule of che::update_evt_ot_et (src/che.cpp:1295-1362):
+	// half-edge he pairs with the first still-free prev(h) among the
+	// half-edges h leaving VT[he] (in half-edge order) with VT[prev(h)] ==
+	// VT[next(he)]; a border vertex whose EVT is a different border
+	// half-edge is non-manifold and gets EVT = NIL.
+	if((nf && (!VT || !OT)) || (nv && !EVT)) return GP_ERR_INVALID_ARG;
+	const uint64_t nhe = 3ull * nf;
+	if(nhe >= 0xFFFFFFFFull) return GP_ERR_INVALID_ARG;
+	for(uint64_t he = 0; he < nhe; he++)
+		if(VT[he] >= nv) return GP_ERR_INVALID_ARG;
+	std::fill(EVT, EVT + nv, NIL);
+	if(manifold) *manifold = 1;
+	if(!nf) return GP_OK;
+	std::vector<uint32_t> start(nv + 1, 0), byv(nhe);
+	for(uint64_t he = 0; he < nhe; he++)
+	{
+		EVT[VT[he]] = (uint32_t) he;
+		start[VT[he] + 1]++;
+	}
+	for(uint32_t v = 0; v < nv; v++) start[v + 1] += start[v];
+	{
+		std::vector<uint32_t> fill(start.begin(), start.end() - 1);
+		for(uint64_t he = 0; he < nhe; he++) byv[fill[VT[he]]++] = (uint32_t) he;
+	}
+	std::fill(OT, OT + nhe, NIL);
+	for(uint32_t he = 0; he < nhe; he++)
+	{
+		if(OT[he] != NIL) continue;
+		const uint32_t a = VT[he], b = VT[he_next(he)];
+		for(uint32_t k = start[a]; k < start[a + 1]; k++)
+		{
+			const uint32_t ph = he_prev(byv[k]);
+			if(VT[ph] == b && OT[he] == NIL && OT[ph] == NIL)
+			{
+				OT[he] = ph;
+				OT[ph] = he;
+			}
+		}
+	}
+	for(uint32_t he = 0; he < nhe; he++)
+	{
+		const uint32_t v = VT[he];
+		if(OT[he] != NIL || EVT[v] == NIL) continue;
+		if(OT[EVT[v]] == NIL && EVT[v] != he)
+		{
+			EVT[v] = NIL;
+			if(manifold) *manifold = 0;
+		}
+		else EVT[v] = he;
+	}
+	return GP_OK;
+}
+
+gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t nf, const uint32_t *VT,
+                         const uint32_t *OT, const uint32_t *EVT, gp_mesh **out)
+{
+	if(!ctx || !out || !xyz || !nv || (nf && !VT)) return GP_ERR_INVALID_ARG;
+	*out = nullptr;
+	if((uint64_t) 3 * nf >= 0x7FFFFFFFull || nv >= 0x7FFFFFFFu)
+	{
+		set_err(ctx, "mesh too large");
+		return GP_ERR_CAPACITY;
+	}
+	const uint32_t nhe = 3 * nf;
+	std::vector<uint32_t> ot_b, evt_b;
+	if(!OT || !EVT)
+	{
+		ot_b.resize(nhe);
+		evt_b.resize(nv);
+		gp_status s0 = gp_che_build(nv, nf, VT, ot_b.data(), evt_b.data(), nullptr);
+		if(s0 != GP_OK)
+		{
+			set_err(ctx, "gp_che_build failed: a triangle references a vertex out of range");
+			return s0;
+		}
+		OT = ot_b.data();
+		EVT = evt_b.data();
+	}
+	else
+	{
+		for(uint32_t he = 0; he < nhe; he++)
+			if(VT[he] >= nv || (OT[he] != NIL && OT[he] >= nhe))
+			{
+				set_err(ctx, "VT/OT entry %u out of range", he);
+				return GP_ERR_INVALID_ARG;
+			}
+		for(uint32_t v = 0; v < nv; v++)
+			if(EVT[v] != NIL && EVT[v] >= nhe)
+			{
+				set_err(ctx, "EVT[%u] out of range", v);
+				return GP_ERR_INVALID_ARG;
+			}
+	}
+	GP_CUDA(ctx, cudaSetDevice(ctx->device));
+	cudaStream_t s = ctx->stream;
+	// temporaries: VT, OT, EVT, counts (+flags), scan scratch, xyz, err
+	Carve tc;
+	const size_t t_vt = tc.add<uint32_t>(nhe), t_ot = tc.add<uint32_t>(nhe), t_evt = tc.add<uint32_t>(nv);
+	const size_t t_cnt = tc.add<uint32_t>(nv + 1), t_flags = tc.add<uint32_t>(nv);
+	const size_t t_scan = tc.add<uint32_t>(scan_tmp_words(nv)), t_xyz = tc.add<double>(3 * (size_t) nv);
+	const size_t t_err = tc.add<uint32_t>(4);
+	gp_status st = ensure_ws(ctx, tc.off);
+	if(st != GP_OK) return st;
+	char *T = static_cast<char *>(ctx->ws);
+	GP_CUDA(ctx, cudaMemcpyAsync(T + t_vt, VT, 4 * (size_t) nhe, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(T + t_ot, OT, 4 * (size_t) nhe, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(T + t_evt, EVT, 4 * (size_t) nv, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(T + t_xyz, xyz, 24 * (size_t) nv, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemsetAsync(T + t_err, 0, 16, s));
+	uint32_t *dvt = reinterpret_cast<uint32_t *>(T + t_vt), *dot = reinterpret_cast<uint32_t *>(T + t_ot);
+	uint32_t *devt = reinterpret_cast<uint32_t *>(T + t_evt), *dflags = reinterpret_cast<uint32_t *>(T + t_flags);
+	uint32_t *dcnt = reinterpret_cast<uint32_t *>(T + t_cnt), *derr = reinterpret_cast<uint32_t *>(T + t_err);
+	GP_CUDA(ctx, launch_fan_count(dvt, dot, devt, nv, nhe, dflags, derr, s));
+	GP_CUDA(ctx, launch_strip_flags(dflags, dcnt, nv, s));
+	GP_CUDA(ctx, launch_scan_u32(dcnt, dcnt, nv, reinterpret_cast<uint32_t *>(T + t_scan), s));
+	GP_CUDA(ctx, launch_max_u32(dflags, nv, derr + 1, s));
+	uint32_t h[2] = {0, 0}, n_fan = 0;
+	GP_CUDA(ctx, cudaMemcpyAsync(h, derr, 8, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(&n_fan, dcnt + nv, 4, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
+	if(h[0])
+	{
+		set_err(ctx, "mesh: a star walk does not close (err=%u)", h[0]);
+		return h[0] & DEV_ERR_WALK ? GP_ERR_NONMANIFOLD : GP_ERR_INVALID_ARG;
+	}
+	gp_mesh *m = new gp_mesh;
+	m->ctx = ctx;
+	m->nv = nv;
+	m->nf = nf;
+	Carve mc;
+	const size_t m_pos = mc.add<float4>(nv), m_posd = mc.add<double>(4 * (size_t) nv);
+	const size_t m_off = mc.add<uint32_t>(nv + 1), m_fan = mc.add<uint32_t>(n_fan);
+	cudaError_t e = cudaMalloc(&m->block, mc.off);
+	if(e != cudaSuccess)
+	{
+		delete m;
+		set_err(ctx, "cudaMalloc mesh: %s", cudaGetErrorString(e));
+		return GP_ERR_OUT_OF_MEMORY;
+	}
+	char *B = static_cast<char *>(m->block);
+	m->dev.pos = reinterpret_cast<float4 *>(B + m_pos);
+	m->dev.posd = reinterpret_cast<double *>(B + m_posd);
+	m->dev.fan_off = reinterpret_cast<uint32_t *>(B + m_off);
+	m->dev.fan = reinterpret_cast<uint32_t *>(B + m_fan);
+	m->dev.nv = nv;
+	m->dev.n_fan = n_fan;
+	m->dev.max_fan = h[1];
+	uint32_t *doff = const_cast<uint32_t *>(m->dev.fan_off);
+	e = cudaMemcpyAsync(doff, dcnt, 4 * ((size_t) nv + 1), cudaMemcpyDeviceToDevice, s);
+	if(e == cudaSuccess) e = launch_fan_fill(dvt, dot, devt, nv, dflags, doff, const_cast<uint32_t *>(m->dev.fan), s);
+	if(e == cudaSuccess)
+		e = launch_pos_convert(reinterpret_cast<double *>(T + t_xyz), nv, const_cast<float4 *>(m->dev.pos),
+		                       const_cast<double *>(m->dev.posd), s);
+	if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+	if(e != cudaSuccess)
+	{
+		set_err(ctx, "mesh upload: %s", cudaGetErrorString(e));
+		cudaFree(m->block);
+		delete m;
+		return GP_ERR_CUDA;
+	}
+	*out = m;
+	return GP_OK;
+}
+
+void gp_mesh_destroy(gp_mesh *m)
+{
+	// cudaFree waits for work on the buffer; the owning context is not
+	// touched, so meshes may outlive (and be freed after) their context.
+	if(!m) return;
+	if(m->block) cudaFree(m->block);
+	delete m;
+}
+
+uint32_t gp_mesh_n_vertices(const gp_mesh *m) { return m ? m->nv : 0; }
+uint32_t gp_mesh_n_faces(const gp_mesh *m) { return m ? m->nf : 0; }
+
+gp_status gp_toplesets(gp_ctx *ctx, gp_mesh *mesh, const uint32_t *sources, uint32_t n_sources, uint32_t *rings,
+                       uint32_t *sorted, uint32_t cap_sorted, uint32_t *limits, uint32_t cap_limits, uint32_t *n_limits)
+{
+	if(!ctx || !mesh || !sources || !n_sources || !limits || !n_limits) return GP_ERR_INVALID_ARG;
+	Req r{mesh, sources, n_sources, nullptr, 0, nullptr, nullptr, nullptr, nullptr};
+	TopOut t{rings, sorted, cap_sorted, limits, cap_limits, n_limits};
+	return run(ctx, &r, 1, nullptr, GP_F32, false, false, Stage::toplesets, &t, nullptr);
+}
+
+gp_status gp_ptp(gp_ctx *ctx, gp_mesh *mesh, const uint32_t *sources, uint32_t n_sources, const uint32_t *limits,
+                 uint32_t n_limits, const uint32_t *sorted, const gp_ptp_opts *opts, void *dist, gp_dtype dist_type,
+                 uint32_t *clusters, gp_ptp_stats *stats)
+{
+	if(!ctx || !mesh || !dist) return GP_ERR_INVALID_ARG;
+	if((limits == nullptr) != (sorted == nullptr)) return GP_ERR_INVALID_ARG;
+	Req r{mesh, sources, n_sources, limits, n_limits, sorted, dist, clusters, stats};
+	return run(ctx, &r, 1, opts, dist_type, false, false, Stage::ptp, nullptr, nullptr);
+}
+
+gp_status gp_ptp_batch(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, const gp_ptp_opts *opts,
+                       gp_dtype dist_type, uint32_t flags, double *seconds)
+{
+	if(!ctx || (n_fields && !fields)) return GP_ERR_INVALID_ARG;
+	std::vector<Req> reqs(n_fields);
+	for(uint32_t f = 0; f < n_fields; f++)
+		reqs[f] = Req{fields[f].mesh, fields[f].sources, fields[f].n_sources, nullptr, 0, nullptr,
+		              fields[f].dist, fields[f].clusters, fields[f].stats};
+	const bool dev = (flags & GP_BATCH_DEVICE_POINTERS) != 0;
+	return run(ctx, reqs.data(), n_fields, opts, dist_type, dev, dev, Stage::ptp, nullptr, seconds);
+}
+
+gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n)
+{
+	if(!ctx || !dist) return GP_ERR_INVALID_ARG;
+	if(!n) return GP_OK;
+	const size_t sz = dist_type == GP_F64 ? 8 : 4;
+	gp_status st = ensure_ws(ctx, n * sz + 256 + 64);
+	if(st != GP_OK) return st;
+	char *W = static_cast<char *>(ctx->ws);
+	unsigned long long *tmp = reinterpret_cast<unsigned long long *>(W + align_up(n * sz, 256));
+	cudaStream_t s = ctx->stream;
+	GP_CUDA(ctx, cudaMemcpyAsync(W, dist, n * sz, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, launch_normalize(W, dist_type == GP_F64, n, tmp, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(dist, W, n * sz, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
+	return GP_OK;
+}
+
+gp_status gp_fps(gp_ctx *ctx, gp_mesh *mesh, uint32_t *samples, uint32_t n_init, uint32_t cap, uint64_t n,
+                 double radio, const gp_ptp_opts *opts, uint32_t *n_out, double *max_dist, double *seconds)
+{
+	if(!ctx || !mesh || !samples || !n_out || !max_dist || !n_init || n_init > cap) return GP_ERR_INVALID_ARG;
+	for(uint32_t k = 0; k < n_init; k++)
+		if(samples[k] >= mesh->nv) return GP_ERR_INVALID_ARG;
+	// farthest_point_sampling_ptp_gpu (src/cuda/geodesics_ptp.cu:122-147)
+	if(n >= mesh->nv) n = mesh->nv >> 1;
+	n = n > n_init ? n - n_init : 0;  // the reference underflows when n < |samples|
+	uint32_t ns = n_init;
+	double md = INFINITY, total = 0;
+	std::vector<float> df;
+	std::vector<double> dd;
+	const bool f64 = opts && opts->precision == GP_F64;
+	// distances stay on the device: a device buffer from the workspace tail is
+	// not possible (run() reuses it), so use a dedicated allocation
+	void *ddist = nullptr;
+	unsigned long long *dmax = nullptr;
+	GP_CUDA(ctx, cudaMalloc(&ddist, (size_t) mesh->nv * (f64 ? 8 : 4)));
+	cudaError_t e0 = cudaMalloc(&dmax, 16);
+	if(e0 != cudaSuccess)
+	{
+		cudaFree(ddist);
+		set_err(ctx, "cudaMalloc: %s", cudaGetErrorString(e0));
+		return GP_ERR_OUT_OF_MEMORY;
+	}
+	gp_status st = GP_OK;
+	while(n-- && md > radio && ns < cap)
+	{
+		Req r{mesh, samples, ns, nullptr, 0, nullptr, ddist, nullptr, nullptr};
+		double sec = 0;
+		// sources are host values; outputs stay on the device
+		st = run(ctx, &r, 1, opts, f64 ? GP_F64 : GP_F32, false, true, Stage::ptp, nullptr, &sec);
+		if(st != GP_OK) break;
+		total += sec;
+		unsigned long long h[2];
+		if(launch_argmax_abs(ddist, f64, mesh->nv, dmax, ctx->stream) != cudaSuccess ||
+		   cudaMemcpyAsync(h, dmax, 16, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
+		   cudaStreamSynchronize(ctx->stream) != cudaSuccess)
+		{
+			set_err(ctx, "fps argmax failed");
+			st = GP_ERR_CUDA;
+			break;
+		}
+		const uint32_t fidx = (uint32_t) h[1];
+		if(radio > 0 || !n) std::memcpy(&md, &h[0], sizeof(double));
+		samples[ns++] = fidx;
+	}
+	cudaFree(ddist);
+	cudaFree(dmax);
+	*n_out = ns;
+	*max_dist = md;
+	if(seconds) *seconds = total;
+	return st;
+}
+
+} // extern "C"

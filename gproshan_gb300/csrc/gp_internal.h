@@ -1,0 +1,133 @@
+// Internal types shared by the host glue (gp_capi.cpp) and the CUDA kernels.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gp_ptp.h"
+
+namespace gp {
+
+constexpr uint32_t NIL = 0xFFFFFFFFu;
+constexpr uint32_t FAN_CLOSED = 0x80000000u;  // bit 31 of fan_off[v]: v's fan is closed
+constexpr uint32_t FAN_MASK = 0x7FFFFFFFu;
+constexpr uint32_t MAX_WALK = 1u << 16;       // longest star walk accepted per vertex
+
+// trig/next/prev of the compact half-edge mesh (src/che.cpp:18-34)
+__host__ __device__ inline uint32_t he_next(uint32_t he) { return 3 * (he / 3) + (he + 1) % 3; }
+__host__ __device__ inline uint32_t he_prev(uint32_t he) { return 3 * (he / 3) + (he + 2) % 3; }
+
+// device error bits (GridSync::err)
+constexpr uint32_t DEV_ERR_TIMEOUT = 1u;   // a grid-barrier wait ran past its limit
+constexpr uint32_t DEV_ERR_WALK = 2u;      // a star walk did not close
+constexpr uint32_t DEV_ERR_BOUNDS = 4u;    // an index outside its buffer
+
+// Barrier / abort word of one persistent launch.
+struct GridSync {
+	uint32_t count;  // CTAs arrived at the current barrier
+	uint32_t gen;    // barrier generation
+	uint32_t err;    // DEV_ERR_* bits
+	uint32_t abort;  // set once any CTA gives up; the others leave at their next barrier
+};
+
+// A mesh on the device, original vertex numbering.
+struct MeshDev {
+	const float4 *pos;       // nv (x, y, z, 0)
+	const double *posd;      // 4*nv (x, y, z, 0); null unless the FP64 path is enabled
+	const uint32_t *fan_off; // nv+1; entries [fan_off[v]&MASK, fan_off[v+1]&MASK); bit31 = closed
+	const uint32_t *fan;     // link of each vertex in star-walk order (che::link order)
+	uint32_t nv;
+	uint32_t n_fan;
+	uint32_t max_fan;        // largest per-vertex entry count
+	uint32_t pad;
+};
+
+// Buffers of one field (one source set on one mesh) on the device.
+struct FieldDev {
+	MeshDev m;
+	const uint32_t *src;      // ns sources
+	uint32_t ns;
+	uint32_t cap_sorted;      // nv + ns
+	// toplesets
+	uint32_t *ring;           // nv
+	unsigned long long *key;  // nv: BFS discovery key (frontier position << 20 | link slot)
+	uint32_t *sorted;         // cap_sorted
+	uint32_t *limits;         // nv + 2
+	// ring-renumbered copy: new id k = position k of sorted; id nr = "unreached" sentinel
+	uint32_t *inv;            // nv: old -> new id (sentinel if unreached)
+	float4 *P;                // cap_sorted + 1
+	double *Pd;               // 4*(cap_sorted + 1) or null
+	uint32_t *off;            // cap_sorted + 2 (bit31 = closed)
+	uint32_t *fan;            // renumbered fan entries
+	void *D[2];               // cap_sorted + 1 distances (float or double)
+	uint32_t *C[2];           // cap_sorted + 1 labels, or null
+	// outputs / inputs in original numbering
+	void *dist_out;           // nv of out_dtype
+	uint32_t *clusters_out;   // nv or null
+	const uint32_t *clusters_in; // nv initial labels or null
+	uint32_t *trace;          // 2 * trace_cap (i, j) per sweep or null
+	uint32_t trace_cap;
+	uint32_t out_f64;         // 1: dist_out is double
+	uint32_t max_iter;        // 0: 2 * n_limits
+	uint32_t pad;
+	double tol;
+};
+
+// Mutable per-field state of the persistent launches.
+struct FieldState {
+	// toplesets
+	uint32_t level;      // ring index of the current frontier
+	uint32_t n_limits;   // |limits| once the BFS is finished
+	uint32_t bfs_live;   // 1 while the BFS of this field runs
+	uint32_t status;     // DEV_ERR_* of this field
+	uint32_t bfs_next;   // size of the ring found by the current BFS level
+	// PTP schedule (run_ptp_gpu, src/cuda/geodesics_ptp.cu:198-229)
+	uint32_t i, j, d, iter, max_iter, n_iter, live, notok;
+	uint32_t win_s, win_e, chk_e, nr;
+	uint32_t big;        // 1: swept by the grid-wide launch, 0: by one CTA
+	uint32_t bound;      // largest window the schedule can open: max_j limits[j] - limits[j/2]
+	unsigned long long relax;
+};
+
+// Host-visible description of a batch plan (all in one device allocation).
+struct PlanDev {
+	uint32_t n_act;        // active fields this step
+	uint32_t total_tiles;  // tiles of this step
+	uint32_t live;         // any field still running
+	uint32_t step;         // steps taken
+	uint32_t *act;         // F: active field ids
+	uint32_t *tile_start;  // F + 1: first tile of each active field
+	uint32_t *tile_aux;    // per-tile scratch (BFS tile counts / bases)
+	uint32_t cap_tiles;
+	uint32_t pad;
+};
+
+// ------------------------------------------------------------------
+// Kernel entry points implemented in the .cu files (all asynchronous on `s`).
+// ------------------------------------------------------------------
+
+// gp_mesh.cu
+cudaError_t launch_fan_count(const uint32_t *VT, const uint32_t *OT, const uint32_t *EVT, uint32_t nv,
+                             uint32_t nhe, uint32_t *cnt, uint32_t *err, cudaStream_t s);
+cudaError_t launch_pos_convert(const double *xyz, uint32_t nv, float4 *pos, double *posd, cudaStream_t s);
+
+// exclusive scan of n u32 values (in place allowed); out[n] receives the total.
+// tmp needs scan_tmp_words(n) words.
+size_t scan_tmp_words(size_t n);
+cudaError_t launch_scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *tmp, cudaStream_t s);
+cudaError_t launch_max_u32(const uint32_t *in, size_t n, uint32_t *out, cudaStream_t s);
+
+// gp_toplesets.cu: BFS of all fields; fills ring/sorted/limits and state[f].n_limits.
+cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
+                             uint32_t ctas, cudaStream_t s);
+int toplesets_max_ctas(int device);
+
+// gp_ptp.cu
+cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, PlanDev *plan,
+                       GridSync *sync, uint32_t ctas, bool f64, bool clusters, cudaStream_t s);
+int ptp_max_ctas(int device, bool f64, bool clusters);
+cudaError_t launch_argmax_abs(const void *dist, bool f64, uint32_t n, unsigned long long *out,
+                              cudaStream_t s);
+
+} // namespace gp

@@ -1,0 +1,232 @@
+// Mesh upload kernels: star lists ("fans") built from the compact half-edge
+// tables, coordinate conversion, and the device scan used by every layout pass.
+//
+// A vertex's fan is the sequence of link vertices met by the reference's star
+// walk (for_star, include/che.h:10): for each half-edge he of the star, in walk
+// order, the vertex VT[next(he)]; when the walk ends on a border
+// (OT[prev(he)] == NIL) the last VT[prev(he)] follows.  This is exactly
+// che::link (src/che.cpp:102-112), so the BFS reads it as the link, and the
+// relaxation reads consecutive pairs as the star triangles (x0 = VT[next(he)],
+// x1 = VT[prev(he)], src/geodesics_ptp.cpp:203-205): on a closed fan the last
+// pair wraps to the first entry.
+#include "gp_common.cuh"
+
+namespace gp {
+
+namespace {
+
+constexpr int SCAN_NT = 256;
+constexpr int SCAN_IPT = 4;
+constexpr int SCAN_TILE = SCAN_NT * SCAN_IPT;
+
+__global__ void fan_count_kernel(const uint32_t *__restrict__ VT, const uint32_t *__restrict__ OT,
+                                 const uint32_t *__restrict__ EVT, uint32_t nv, uint32_t nhe,
+                                 uint32_t *__restrict__ cnt, uint32_t *__restrict__ err)
+{
+	const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+	if(v >= nv) return;
+	const uint32_t he0 = EVT[v];
+	uint32_t c = 0, closed = 0;
+	if(he0 != NIL)
+	{
+		if(he0 >= nhe) { atomicOr(err, DEV_ERR_BOUNDS); cnt[v] = 0; return; }
+		uint32_t he = he0, T = 0;
+		for(;;)
+		{
+			T++;
+			const uint32_t nx = OT[he_prev(he)];
+			if(nx == NIL) break;
+			if(nx == he0) { closed = 1; break; }
+			if(nx >= nhe || T >= MAX_WALK) { atomicOr(err, nx >= nhe ? DEV_ERR_BOUNDS : DEV_ERR_WALK); T = 0; break; }
+			he = nx;
+		}
+		c = T ? (closed ? T : T + 1) : 0;
+	}
+	cnt[v] = c | (closed ? FAN_CLOSED : 0u);
+}
+
+__global__ void strip_flag_kernel(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, uint32_t n)
+{
+	const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+	if(v < n) out[v] = in[v] & FAN_MASK;
+}
+
+__global__ void fan_fill_kernel(const uint32_t *__restrict__ VT, const uint32_t *__restrict__ OT,
+                                const uint32_t *__restrict__ EVT, uint32_t nv,
+                                const uint32_t *__restrict__ flags, uint32_t *__restrict__ off,
+                                uint32_t *__restrict__ fan)
+{
+	const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+	if(v >= nv) return;
+	const uint32_t f = flags[v];
+	const uint32_t n = f & FAN_MASK;
+	const uint32_t o = off[v];
+	if(n)
+	{
+		const uint32_t he0 = EVT[v];
+		uint32_t he = he0, k = 0;
+		for(;;)
+		{
+			fan[o + k++] = VT[he_next(he)];
+			const uint32_t nx = OT[he_prev(he)];
+			if(nx == NIL) { fan[o + k++] = VT[he_prev(he)]; break; }
+			if(nx == he0 || k >= n) break;
+			he = nx;
+		}
+	}
+	off[v] = o | (f & FAN_CLOSED);
+}
+
+__global__ void max_kernel(const uint32_t *__restrict__ in, size_t n, uint32_t *out)
+{
+	uint32_t m = 0;
+	for(size_t i = blockIdx.x * (size_t) blockDim.x + threadIdx.x; i < n; i += (size_t) gridDim.x * blockDim.x)
+		m = max(m, in[i] & FAN_MASK);
+	for(int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
+	if((threadIdx.x & 31) == 0) atomicMax(out, m);
+}
+
+__global__ void pos_kernel(const double *__restrict__ xyz, uint32_t nv, float4 *__restrict__ pos,
+                           double *__restrict__ posd)
+{
+	const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+	if(v >= nv) return;
+	const double x = xyz[3 * (size_t) v], y = xyz[3 * (size_t) v + 1], z = xyz[3 * (size_t) v + 2];
+	pos[v] = make_float4((float) x, (float) y, (float) z, 0.f);
+	if(posd)
+	{
+		posd[4 * (size_t) v] = x;
+		posd[4 * (size_t) v + 1] = y;
+		posd[4 * (size_t) v + 2] = z;
+		posd[4 * (size_t) v + 3] = 0.0;
+	}
+}
+
+// --- scan: per-tile sums, recursive scan of the sums, then per-tile scan ----
+
+__global__ void scan_reduce_kernel(const uint32_t *__restrict__ in, size_t n, uint32_t *__restrict__ sums)
+{
+	const size_t base = (size_t) blockIdx.x * SCAN_TILE;
+	uint32_t s = 0;
+#pragma unroll
+	for(int k = 0; k < SCAN_IPT; k++)
+	{
+		const size_t i = base + (size_t) threadIdx.x * SCAN_IPT + k;
+		if(i < n) s += in[i];
+	}
+	for(int o = 16; o; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+	__shared__ uint32_t ws[SCAN_NT / 32];
+	if((threadIdx.x & 31) == 0) ws[threadIdx.x >> 5] = s;
+	__syncthreads();
+	if(threadIdx.x == 0)
+	{
+		uint32_t t = 0;
+		for(int w = 0; w < SCAN_NT / 32; w++) t += ws[w];
+		sums[blockIdx.x] = t;
+	}
+}
+
+__global__ void scan_tile_kernel(const uint32_t *__restrict__ in, uint32_t *__restrict__ out, size_t n,
+                                 const uint32_t *__restrict__ tile_off, int write_total)
+{
+	const size_t base = (size_t) blockIdx.x * SCAN_TILE;
+	uint32_t v[SCAN_IPT];
+	uint32_t s = 0;
+#pragma unroll
+	for(int k = 0; k < SCAN_IPT; k++)
+	{
+		const size_t i = base + (size_t) threadIdx.x * SCAN_IPT + k;
+		v[k] = i < n ? in[i] : 0u;
+		s += v[k];
+	}
+	uint32_t tot;
+	const uint32_t ex = block_exclusive_scan<SCAN_NT>(s, &tot);
+	uint32_t run = ex + (tile_off ? tile_off[blockIdx.x] : 0u);
+#pragma unroll
+	for(int k = 0; k < SCAN_IPT; k++)
+	{
+		const size_t i = base + (size_t) threadIdx.x * SCAN_IPT + k;
+		if(i < n) out[i] = run;
+		run += v[k];
+	}
+	if(write_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_NT - 1) out[n] = run;
+}
+
+} // namespace
+
+size_t scan_tmp_words(size_t n)
+{
+	size_t words = 0;
+	while(n > (size_t) SCAN_TILE)
+	{
+		const size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+		words += nb + 1;
+		n = nb;
+	}
+	return words + 1;
+}
+
+cudaError_t launch_scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *tmp, cudaStream_t s)
+{
+	if(n == 0)
+		return cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
+	if(n <= (size_t) SCAN_TILE)
+	{
+		scan_tile_kernel<<<1, SCAN_NT, 0, s>>>(in, out, n, nullptr, 1);
+		return cudaGetLastError();
+	}
+	const size_t nb = (n + SCAN_TILE - 1) / SCAN_TILE;
+	uint32_t *sums = tmp;          // nb + 1 entries (scanned in place)
+	uint32_t *rest = tmp + nb + 1;
+	scan_reduce_kernel<<<(unsigned) nb, SCAN_NT, 0, s>>>(in, n, sums);
+	cudaError_t e = launch_scan_u32(sums, sums, nb, rest, s);
+	if(e != cudaSuccess) return e;
+	scan_tile_kernel<<<(unsigned) nb, SCAN_NT, 0, s>>>(in, out, n, sums, 1);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_max_u32(const uint32_t *in, size_t n, uint32_t *out, cudaStream_t s)
+{
+	cudaError_t e = cudaMemsetAsync(out, 0, sizeof(uint32_t), s);
+	if(e != cudaSuccess) return e;
+	const unsigned nb = (unsigned) std::min<size_t>((n + 255) / 256 + 1, 4096);
+	max_kernel<<<nb, 256, 0, s>>>(in, n, out);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_fan_count(const uint32_t *VT, const uint32_t *OT, const uint32_t *EVT, uint32_t nv,
+                             uint32_t nhe, uint32_t *cnt, uint32_t *err, cudaStream_t s)
+{
+	if(!nv) return cudaSuccess;
+	fan_count_kernel<<<(nv + 255) / 256, 256, 0, s>>>(VT, OT, EVT, nv, nhe, cnt, err);
+	return cudaGetLastError();
+}
+
+// off[nv+1]: on entry the exclusive scan of the counts; on return bit 31 of
+// off[v] carries the closed flag.  flags[nv] holds count | closed bit.
+cudaError_t launch_fan_fill(const uint32_t *VT, const uint32_t *OT, const uint32_t *EVT, uint32_t nv,
+                            const uint32_t *flags, uint32_t *off, uint32_t *fan, cudaStream_t s);
+
+cudaError_t launch_fan_fill(const uint32_t *VT, const uint32_t *OT, const uint32_t *EVT, uint32_t nv,
+                            const uint32_t *flags, uint32_t *off, uint32_t *fan, cudaStream_t s)
+{
+	if(!nv) return cudaSuccess;
+	fan_fill_kernel<<<(nv + 255) / 256, 256, 0, s>>>(VT, OT, EVT, nv, flags, off, fan);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_strip_flags(const uint32_t *in, uint32_t *out, uint32_t n, cudaStream_t s)
+{
+	if(!n) return cudaSuccess;
+	strip_flag_kernel<<<(n + 255) / 256, 256, 0, s>>>(in, out, n);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_pos_convert(const double *xyz, uint32_t nv, float4 *pos, double *posd, cudaStream_t s)
+{
+	if(!nv) return cudaSuccess;
+	pos_kernel<<<(nv + 255) / 256, 256, 0, s>>>(xyz, nv, pos, posd);
+	return cudaGetLastError();
+}
+
+} // namespace gp

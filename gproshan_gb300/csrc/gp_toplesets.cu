@@ -1,0 +1,179 @@
+// Toplesets (BFS rings) of many fields at once, on the GPU.
+//
+// Restates che::compute_toplesets (src/che.cpp:546-593) over the directed link
+// relation che::link (src/che.cpp:102-112) so that ring indices, limits AND the
+// order of `sorted` equal the reference's bit for bit.
+//
+// The reference appends a newly met vertex u the first time a ring-r vertex
+// lists it, scanning ring r in `sorted` order and each link in link order.  So
+// u's position in ring r+1 is fixed by the smallest key
+// (position of the discovering vertex in `sorted`, slot in its link).
+//
+// One CTA owns one field at a time (fields are taken from a queue), so a level
+// needs only CTA barriers:
+//   discover: atomicMin(key[u], pos << 20 | slot) for every unvisited u;
+//   emit:     frontier chunks in `sorted` order; each vertex counts the u
+//             whose key it holds, a block scan (carried across chunks) gives
+//             their positions, and the owners write them and set ring[u].
+#include "gp_common.cuh"
+
+namespace gp {
+
+namespace {
+
+constexpr int BT = 1024;  // threads of a BFS CTA
+
+// Count (and with EMIT write) the vertices owned by frontier position p.
+template <bool EMIT>
+__device__ __forceinline__ uint32_t own(const FieldDev &F, uint32_t p, uint32_t level, uint32_t out)
+{
+	const uint32_t v = ldcg(F.sorted + p);
+	const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
+	uint32_t c = 0;
+	for(uint32_t e = o0; e < o1; e++)
+	{
+		const uint32_t u = __ldg(F.m.fan + e);
+		const unsigned long long mine = ((unsigned long long) p << 20) | (e - o0);
+		if(ldcg(F.ring + u) == NIL && ldcg(F.key + u) == mine)
+		{
+			if(EMIT)
+			{
+				F.sorted[out + c] = u;
+				F.ring[u] = level + 1;
+			}
+			c++;
+		}
+	}
+	return c;
+}
+
+__global__ void __launch_bounds__(BT) bfs_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields,
+                                                 uint32_t *queue)
+{
+	__shared__ uint32_t s_f;
+	for(;;)
+	{
+		if(threadIdx.x == 0) s_f = atomicAdd(queue, 1u);
+		__syncthreads();
+		const uint32_t f = s_f;
+		__syncthreads();
+		if(f >= n_fields) return;
+		const FieldDev &F = fields[f];
+		if(!state[f].bfs_live) continue;  // no sources, or a source out of range
+
+		uint32_t level = 0, s = 0, e = F.ns;  // frontier = ring 0 = [0, ns)
+		for(;;)
+		{
+			for(uint32_t p = s + threadIdx.x; p < e; p += BT)
+			{
+				const uint32_t v = ldcg(F.sorted + p);
+				const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
+				for(uint32_t q = o0; q < o1; q++)
+				{
+					const uint32_t u = __ldg(F.m.fan + q);
+					if(ldcg(F.ring + u) == NIL) atomicMin(F.key + u, ((unsigned long long) p << 20) | (q - o0));
+				}
+			}
+			__syncthreads();
+			uint32_t carry = 0;
+			for(uint32_t base = s; base < e; base += BT)
+			{
+				const uint32_t p = base + threadIdx.x;
+				const uint32_t c = p < e ? own<false>(F, p, level, 0) : 0u;
+				uint32_t tot;
+				const uint32_t ex = block_exclusive_scan<BT>(c, &tot);
+				if(c) own<true>(F, p, level, e + carry + ex);
+				carry += tot;
+			}
+			__syncthreads();
+			if(!carry) break;
+			if(threadIdx.x == 0) F.limits[level + 2] = e + carry;
+			s = e;
+			e += carry;
+			level++;
+		}
+		if(threadIdx.x == 0)
+		{
+			state[f].n_limits = level + 2;
+			state[f].bfs_live = 0;
+		}
+	}
+}
+
+// Per-field setup: ring = NIL, key = max over the field's vertices.
+__global__ void bfs_clear_kernel(FieldDev *fields, const uint32_t *vbase, uint32_t n_fields, uint32_t total)
+{
+	for(uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < total; g += gridDim.x * blockDim.x)
+	{
+		const uint32_t f = upper_index(vbase, n_fields, g);
+		const uint32_t v = g - vbase[f];
+		fields[f].ring[v] = NIL;
+		fields[f].key[v] = ~0ull;
+	}
+}
+
+// Sources -> ring 0, in the order given (duplicates kept, src/che.cpp:555-561).
+__global__ void bfs_seed_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields)
+{
+	const uint32_t f = blockIdx.x * blockDim.x + threadIdx.x;
+	if(f >= n_fields) return;
+	FieldDev &F = fields[f];
+	FieldState &st = state[f];
+	st.level = 0;
+	st.status = 0;
+	st.bfs_next = 0;
+	for(uint32_t s = 0; s < F.ns; s++)
+		if(F.src[s] >= F.m.nv)
+		{
+			// a source outside the mesh: report it and leave the field empty
+			st.status = DEV_ERR_BOUNDS;
+			st.bfs_live = 0;
+			st.n_limits = 0;
+			return;
+		}
+	for(uint32_t s = 0; s < F.ns; s++)
+	{
+		const uint32_t v = F.src[s];
+		F.sorted[s] = v;
+		F.ring[v] = 0;
+	}
+	F.limits[0] = 0;
+	F.limits[1] = F.ns;
+	st.bfs_live = F.ns > 0;
+	st.n_limits = F.ns > 0 ? 2 : 0;
+}
+
+} // namespace
+
+cudaError_t launch_bfs_setup(FieldDev *fields, FieldState *state, const uint32_t *vbase, uint32_t n_fields,
+                             uint32_t total_vertices, cudaStream_t s)
+{
+	if(total_vertices)
+	{
+		const unsigned nb = (unsigned) std::min<uint32_t>((total_vertices + 255) / 256, 152 * 16);
+		bfs_clear_kernel<<<nb, 256, 0, s>>>(fields, vbase, n_fields, total_vertices);
+	}
+	bfs_seed_kernel<<<(n_fields + 127) / 128, 128, 0, s>>>(fields, state, n_fields);
+	return cudaGetLastError();
+}
+
+int toplesets_max_ctas(int device)
+{
+	int nsm = 0, per = 0;
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bfs_kernel, BT, 0);
+	return nsm * per;
+}
+
+// queue: one word, zeroed here (the field ticket)
+cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
+                             uint32_t ctas, cudaStream_t s)
+{
+	cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
+	if(e != cudaSuccess) return e;
+	ctas = std::max<uint32_t>(1, std::min<uint32_t>(ctas, n_fields));
+	bfs_kernel<<<ctas, BT, 0, s>>>(fields, state, n_fields, queue);
+	return cudaGetLastError();
+}
+
+} // namespace gp

@@ -1,0 +1,187 @@
+/*
+ * gp_ptp.h -- C ABI of the GB300-native Parallel Toplesets Propagation (PTP)
+ * geodesics library (libgp_ptp.so).
+ *
+ * This is the drop-in boundary for gproshan's PTP_GPU path.  Every entry point
+ * takes plain pointers and sizes, returns a gp_status, never calls
+ * cudaDeviceReset and never aborts the process.  Each one lists the reference
+ * interface it replaces (paths are inside the gproshan source tree).
+ *
+ * Types follow the reference: index_t = uint32_t, NIL = 0xFFFFFFFF
+ * (include/include.h:12,19).  Distances are float (the reference's SINGLE_P
+ * build) or double (its default build); the caller picks per call.
+ *
+ * Threading: one gp_ctx per thread (a context owns one CUDA stream and a
+ * workspace); meshes belong to the context that made them.  Calls on one
+ * context are serialised by the caller.
+ */
+#ifndef GP_PTP_H
+#define GP_PTP_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GP_NIL 0xFFFFFFFFu
+#define GP_PTP_TOL 1e-3 /* PTP_TOL, include/geodesics_ptp.h:11 */
+
+typedef enum gp_status {
+	GP_OK = 0,
+	GP_ERR_INVALID_ARG = 1,     /* null pointer, size out of range, bad vertex index */
+	GP_ERR_NONMANIFOLD = 2,     /* a star walk does not close within the mesh size */
+	GP_ERR_NO_CONVERGENCE = 3,  /* reserved: the reference stops at max_iter silently */
+	GP_ERR_DEVICE_TIMEOUT = 4,  /* a device-side wait ran past its limit */
+	GP_ERR_CUDA = 5,            /* a CUDA runtime call failed; see gp_ctx_last_error */
+	GP_ERR_NO_DEVICE = 6,       /* no CUDA device / not an sm_103 device */
+	GP_ERR_OUT_OF_MEMORY = 7,
+	GP_ERR_CAPACITY = 8         /* an output buffer is too small */
+} gp_status;
+
+typedef enum gp_dtype { GP_F32 = 0, GP_F64 = 1 } gp_dtype;
+
+typedef struct gp_ctx gp_ctx;
+typedef struct gp_mesh gp_mesh;
+
+/* ------------------------------------------------------------------ */
+/* context                                                             */
+/* ------------------------------------------------------------------ */
+
+/* Create a context on CUDA device `device` (one stream, one workspace).
+ * Replaces the per-call cudaDeviceReset + cudaMalloc of
+ * src/cuda/geodesics_ptp.cu:22-46 with a reusable workspace. */
+gp_status gp_ctx_create(int device, gp_ctx **out);
+void gp_ctx_destroy(gp_ctx *ctx);
+/* Text of the last error seen by this context ("" if none). */
+const char *gp_ctx_last_error(const gp_ctx *ctx);
+const char *gp_status_str(gp_status s);
+/* The context's cudaStream_t, as void*. */
+void *gp_ctx_stream(gp_ctx *ctx);
+/* Bytes of device workspace currently held by the context. */
+size_t gp_ctx_workspace_bytes(const gp_ctx *ctx);
+
+/* ------------------------------------------------------------------ */
+/* mesh                                                                */
+/* ------------------------------------------------------------------ */
+
+/* Host-side compact half-edge build: opposite table OT[3*n_faces] and extra
+ * vertex table EVT[n_vertices] from VT[3*n_faces], with the reference's
+ * matching and non-manifold rules (che::update_evt_ot_et, src/che.cpp:1295-1362).
+ * *manifold (may be null) receives 1 or 0. */
+gp_status gp_che_build(uint32_t n_vertices, uint32_t n_faces, const uint32_t *VT,
+                       uint32_t *OT, uint32_t *EVT, int *manifold);
+
+/* Upload a CHE mesh (host arrays: xyz[3*n_vertices], VT/OT[3*n_faces],
+ * EVT[n_vertices]) and build its device star lists.  Coordinates are kept as
+ * float (FP32 path) and double (FP64 path).  OT/EVT may be null, in which case
+ * they are built with gp_che_build.
+ * Replaces cuda_create_CHE (src/cuda/che.cu:29-48) and CHE::CHE
+ * (src/che.cpp:36-46). */
+gp_status gp_mesh_create(gp_ctx *ctx, uint32_t n_vertices, const double *xyz,
+                         uint32_t n_faces, const uint32_t *VT, const uint32_t *OT,
+                         const uint32_t *EVT, gp_mesh **out);
+void gp_mesh_destroy(gp_mesh *mesh);
+uint32_t gp_mesh_n_vertices(const gp_mesh *mesh);
+uint32_t gp_mesh_n_faces(const gp_mesh *mesh);
+
+/* ------------------------------------------------------------------ */
+/* toplesets                                                           */
+/* ------------------------------------------------------------------ */
+
+/* Multi-source BFS over the mesh's directed link relation, on the GPU.
+ * rings[n_vertices]: ring index per vertex (NIL if unreached);
+ * sorted[cap_sorted]: vertices in BFS order (sources repeat if given twice);
+ * limits[cap_limits]: start of each ring, then the end.  Output equals
+ * che::compute_toplesets bit for bit (src/che.cpp:546-593, link at 102-112).
+ * Host buffers; any of rings/sorted may be null. */
+gp_status gp_toplesets(gp_ctx *ctx, gp_mesh *mesh, const uint32_t *sources, uint32_t n_sources,
+                       uint32_t *rings, uint32_t *sorted, uint32_t cap_sorted,
+                       uint32_t *limits, uint32_t cap_limits, uint32_t *n_limits);
+
+/* ------------------------------------------------------------------ */
+/* PTP                                                                 */
+/* ------------------------------------------------------------------ */
+
+typedef struct gp_ptp_opts {
+	uint32_t precision;    /* GP_F32 (closed-form FP32 update) or GP_F64 (reference formula) */
+	uint32_t max_iter;     /* 0: the reference's 2*|limits| (src/cuda/geodesics_ptp.cu:204) */
+	double tol;            /* 0: PTP_TOL */
+	uint32_t threads;      /* reserved (threads per CTA are fixed per kernel) */
+	uint32_t ctas;         /* CTAs of the grid-wide launch, 0: all that fit */
+	uint32_t local_window; /* fields whose windows stay within this many vertices are
+	                          swept by one CTA each; 0: default (4096) */
+	uint32_t reserved[3];
+} gp_ptp_opts;
+
+typedef struct gp_ptp_stats {
+	uint32_t n_iter;       /* sweeps run */
+	uint32_t n_limits;     /* |limits| of the toplesets used */
+	uint64_t relaxations;  /* vertex relaxations (sum of window sizes) */
+	double seconds;        /* device time of the call (CUDA events) */
+} gp_ptp_stats;
+
+/*
+ * Geodesic distances from `sources` (host array).
+ *
+ * toplesets: limits/sorted as che::compute_toplesets returns them (host
+ * arrays), or both null to build them on the GPU.
+ * dist: host array of n_vertices elements of type dist_type; unreached
+ * vertices get INFINITY.  clusters (may be null): host array of n_vertices
+ * labels; on entry it holds the initial labels, on return source k's region
+ * carries k+1 (GPU rule, src/cuda/geodesics_ptp.cu:257-282).
+ *
+ * Replaces parallel_toplesets_propagation_gpu (src/cuda/geodesics_ptp.cu:20-85)
+ * and parallel_toplesets_propagation_coalescence_gpu
+ * (src/cuda/geodesics_ptp_coalescence.cu:21-100): the result is the buffer
+ * the last sweep wrote, as those return.
+ */
+gp_status gp_ptp(gp_ctx *ctx, gp_mesh *mesh, const uint32_t *sources, uint32_t n_sources,
+                 const uint32_t *limits, uint32_t n_limits, const uint32_t *sorted,
+                 const gp_ptp_opts *opts, void *dist, gp_dtype dist_type,
+                 uint32_t *clusters, gp_ptp_stats *stats);
+
+/* One field of a batch. */
+typedef struct gp_field {
+	gp_mesh *mesh;
+	const uint32_t *sources;   /* n_sources vertex ids */
+	uint32_t n_sources;
+	void *dist;                /* n_vertices outputs of the batch's dist_type */
+	uint32_t *clusters;        /* null or n_vertices labels (in/out) */
+	gp_ptp_stats *stats;       /* null or per-field statistics */
+} gp_field;
+
+#define GP_BATCH_DEVICE_POINTERS 1u /* sources/dist/clusters are device pointers */
+
+/*
+ * Many independent fields (any meshes, any source sets) solved together: the
+ * GPU toplesets of every field, then one persistent launch that sweeps the
+ * windows of all live fields each step.  Each field's result equals what
+ * gp_ptp returns for it alone.  No reference counterpart: the reference runs
+ * one field per call (src/cuda/geodesics_ptp.cu:20).
+ */
+gp_status gp_ptp_batch(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields,
+                       const gp_ptp_opts *opts, gp_dtype dist_type, uint32_t flags,
+                       double *seconds);
+
+/* normalize_ptp (src/geodesics_ptp.cpp:264-276) on a host array. */
+gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n);
+
+/*
+ * Farthest-point sampling by repeated multi-source PTP
+ * (farthest_point_sampling_ptp_gpu, src/cuda/geodesics_ptp.cu:87-172).
+ * samples: host array of capacity cap holding n_init seeds on entry.
+ * n: requested number of samples (clamped to n_vertices/2 as the reference
+ * does); stops early once the farthest distance drops to radio or below.
+ * *n_out receives the number of samples, *max_dist the last farthest distance.
+ */
+gp_status gp_fps(gp_ctx *ctx, gp_mesh *mesh, uint32_t *samples, uint32_t n_init, uint32_t cap,
+                 uint64_t n, double radio, const gp_ptp_opts *opts, uint32_t *n_out,
+                 double *max_dist, double *seconds);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GP_PTP_H */

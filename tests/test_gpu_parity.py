@@ -1,0 +1,203 @@
+"""GPU parity: the CUDA path through the C ABI against the CPU oracle and the
+golden vectors of the reference's own code.
+
+Bars: integer outputs (rings, sorted, limits, labels, samples) bit-exact; the
+FP64 path (reference formula) bit-exact with the FP64 oracle; the FP32 path
+within max relative error 1e-5 of the FP64 oracle run on the same
+float-rounded coordinates, with the same number of sweeps."""
+import numpy as np
+import pytest
+
+from conftest import golden_cases
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+REL_TOL_F32 = 1e-5
+
+
+def dev_mesh(ctx, xyz, tri):
+    from gproshan_gb300 import _capi
+    return _capi.DeviceMesh(ctx, xyz, tri)
+
+
+@pytest.mark.parametrize("name,g", CASES, ids=[c[0] for c in CASES])
+def test_toplesets_bit_exact_golden(gpu_ctx, name, g):
+    from gproshan_gb300 import _capi
+    m = _capi.DeviceMesh(gpu_ctx, g["xyz"], g["VT"], g["OT"], g["EVT"])
+    for k in range(int(g["n_sets"])):
+        rings, srt, lim = _capi.toplesets(m, g[f"src{k}"])
+        assert np.array_equal(rings, g[f"rings{k}"]), (name, k)
+        assert np.array_equal(lim, g[f"limits{k}"]), (name, k)
+        assert np.array_equal(srt, g[f"sorted{k}"]), (name, k)
+
+
+@pytest.mark.parametrize("name,g", CASES, ids=[c[0] for c in CASES])
+def test_ptp_f64_bit_exact_oracle(gpu_ctx, oracle_lib, name, g):
+    from gproshan_gb300 import _capi
+    m = dev_mesh(gpu_ctx, g["xyz"], g["tri"])
+    om = oracle_lib.Mesh(g["xyz"], g["tri"])
+    for k in range(int(g["n_sets"])):
+        src = g[f"src{k}"]
+        ref = oracle_lib.ptp(om, src, g[f"limits{k}"], g[f"sorted{k}"])
+        d, _, st = _capi.ptp(m, src, dtype=np.float64, precision=_capi.GP_F64)
+        assert st.n_iter == ref["n_iter"], (name, k)
+        assert st.relaxations == ref["relaxations"], (name, k)
+        assert np.array_equal(d, ref["dist"]), (name, k, np.nanmax(np.abs(d - ref["dist"])))
+
+
+@pytest.mark.parametrize("name,g", CASES, ids=[c[0] for c in CASES])
+def test_ptp_f32_within_tolerance(gpu_ctx, oracle_lib, name, g):
+    from gproshan_gb300 import _capi
+    m = dev_mesh(gpu_ctx, g["xyz"], g["tri"])
+    om = oracle_lib.Mesh(g["xyz"], g["tri"])
+    x32 = g["xyz"].astype(np.float32).astype(np.float64)
+    for k in range(int(g["n_sets"])):
+        src = g[f"src{k}"]
+        ref = oracle_lib.ptp(om, src, g[f"limits{k}"], g[f"sorted{k}"], xyz=x32)
+        d, _, st = _capi.ptp(m, src)
+        assert st.n_iter == ref["n_iter"], (name, k)
+        err = oracle_lib.max_rel_err(d, ref["dist"])
+        assert err <= REL_TOL_F32, (name, k, err)
+
+
+def test_caller_toplesets_equal_gpu_toplesets(gpu_ctx):
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.height_field(48, 5)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    rings, srt, lim = _capi.toplesets(m, [7, 1500])
+    a, _, sa = _capi.ptp(m, [7, 1500], lim, srt)
+    b, _, sb = _capi.ptp(m, [7, 1500])
+    assert np.array_equal(a, b) and sa.n_iter == sb.n_iter
+
+
+@pytest.mark.parametrize("maker,src", [
+    (lambda mg: mg.icosphere(5, 0.1, 3), [0]),
+    (lambda mg: mg.height_field(160, 9), [0, 12345, 20000]),
+    (lambda mg: mg.torus(120, 40, seed=2), [5]),
+    (lambda mg: mg.bump_field(90, 4), [77]),
+])
+def test_larger_meshes_against_oracle(gpu_ctx, oracle_lib, maker, src):
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = maker(meshgen)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    r_o, s_o, l_o = oracle_lib.toplesets(om, src)
+    rings, srt, lim = _capi.toplesets(m, src)
+    assert np.array_equal(rings, r_o) and np.array_equal(srt, s_o) and np.array_equal(lim, l_o)
+    ref64 = oracle_lib.ptp(om, src, l_o, s_o)
+    d64, _, st = _capi.ptp(m, src, dtype=np.float64, precision=_capi.GP_F64)
+    assert st.n_iter == ref64["n_iter"] and np.array_equal(d64, ref64["dist"])
+    ref = oracle_lib.ptp(om, src, l_o, s_o, xyz=xyz.astype(np.float32).astype(np.float64))
+    d32, _, st32 = _capi.ptp(m, src)
+    assert st32.n_iter == ref["n_iter"]
+    assert oracle_lib.max_rel_err(d32, ref["dist"]) <= REL_TOL_F32
+
+
+def test_duplicate_and_isolated_sources(gpu_ctx, oracle_lib):
+    from gproshan_gb300 import _capi
+    g = dict(np.load(__import__("os").path.join(__import__("conftest").GOLDEN, "grid_hole.npz")))
+    m = dev_mesh(gpu_ctx, g["xyz"], g["tri"])
+    om = oracle_lib.Mesh(g["xyz"], g["tri"])
+    # isolated source: no sweep, the source at 0, everything else INF
+    d, _, st = _capi.ptp(m, g["src2"], dtype=np.float64, precision=_capi.GP_F64)
+    assert st.n_iter == 0 and d[g["src2"][0]] == 0 and np.isinf(np.delete(d, g["src2"][0])).all()
+    # repeated sources: defined here (every sorted entry is relaxed)
+    src = [168, 5, 168]
+    ref = oracle_lib.ptp(om, src)
+    d, _, st = _capi.ptp(m, src, dtype=np.float64, precision=_capi.GP_F64)
+    assert st.n_iter == ref["n_iter"] and np.array_equal(d, ref["dist"])
+
+
+def test_clusters_gpu_rule(gpu_ctx, oracle_lib):
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.icosphere(4, 0.1, 2)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    src = [0, 1000, 2000]
+    ref = oracle_lib.ptp(om, src, clusters=True)
+    d, cl, _ = _capi.ptp(m, src, dtype=np.float64, precision=_capi.GP_F64,
+                         clusters=np.zeros(len(xyz), np.uint32))
+    assert np.array_equal(d, ref["dist"])
+    assert np.array_equal(cl, ref["clusters"])
+    assert set(np.unique(cl)) == {1, 2, 3}
+
+
+def test_batch_equals_single_fields(gpu_ctx):
+    from gproshan_gb300 import _capi, meshgen
+    meshes = [dev_mesh(gpu_ctx, *meshgen.icosphere(3, 0.1, 1)), dev_mesh(gpu_ctx, *meshgen.height_field(70, 2)),
+              dev_mesh(gpu_ctx, *meshgen.icosphere(5, 0.1, 3)), dev_mesh(gpu_ctx, *meshgen.height_field(33, 8))]
+    rng = np.random.default_rng(0)
+    ms, srcs = [], []
+    for k in range(12):
+        mm = meshes[k % len(meshes)]
+        ms.append(mm)
+        srcs.append(rng.choice(mm.n_vertices, size=1 + k % 3, replace=False))
+    dists, stats, sec = _capi.ptp_batch(gpu_ctx, ms, srcs)
+    assert sec > 0
+    for k in range(12):
+        d, _, st = _capi.ptp(ms[k], srcs[k])
+        assert np.array_equal(d, dists[k]), k
+        assert st.n_iter == stats[k].n_iter
+
+
+def test_fps_matches_oracle(gpu_ctx, oracle_lib):
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.icosphere(3, 0.1, 5)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    s_ref, md_ref = oracle_lib.fps(om, 12, [0])
+    s, md, _ = _capi.fps(m, 12, [0], precision=_capi.GP_F64)
+    assert np.array_equal(s, s_ref) and md == md_ref
+
+
+def test_normalize_matches_oracle(gpu_ctx, oracle_lib):
+    from gproshan_gb300 import _capi
+    rng = np.random.default_rng(3)
+    d = rng.random(1000) * 5
+    d[7] = np.inf
+    out = _capi.normalize_ptp(gpu_ctx, d.copy())
+    ref = oracle_lib.normalize_ptp(d)
+    assert np.array_equal(out, ref)
+
+
+def test_geodesics_api_end_to_end(gpu_ctx, oracle_lib):
+    from gproshan_gb300 import che, geodesics, meshgen, parallel_toplesets_propagation_gpu, ptp_out_t, toplesets_t
+    xyz, tri = meshgen.icosphere(4, 0.1, 9)
+    mesh = che(xyz, tri)
+    g = geodesics(mesh, [3], geodesics.PTP_GPU, ctx=gpu_ctx)
+    om = oracle_lib.Mesh(xyz, tri)
+    ref = oracle_lib.ptp(om, [3], xyz=xyz.astype(np.float32).astype(np.float64))
+    assert oracle_lib.max_rel_err(g.dist, ref["dist"]) <= REL_TOL_F32
+    assert g[3] == 0.0
+    rings, srt, lim = mesh.compute_toplesets([3], ctx=gpu_ctx)
+    out = ptp_out_t(np.empty(mesh.n_vertices(), np.float64))
+    t = parallel_toplesets_propagation_gpu(out, mesh, [3], toplesets_t(lim, srt), ctx=gpu_ctx)
+    assert t > 0 and np.array_equal(out.dist, g.dist)
+
+
+def test_invalid_source_is_an_error_and_context_survives(gpu_ctx):
+    from gproshan_gb300 import _capi, meshgen
+    m = dev_mesh(gpu_ctx, *meshgen.icosphere(2, 0.0, 0))
+    with pytest.raises(_capi.GPError) as e:
+        _capi.ptp(m, [m.n_vertices + 5])
+    assert e.value.status == 1
+    d, _, _ = _capi.ptp(m, [0])
+    assert d[0] == 0 and np.isfinite(d).all()
+
+
+@pytest.mark.parametrize("maker,src", [
+    (lambda mg: mg.icosphere(4, 0.1, 1), [0]),
+    (lambda mg: mg.height_field(96, 6), [5, 4000]),
+])
+@pytest.mark.parametrize("precision", [0, 1])
+def test_one_cta_and_grid_paths_agree(gpu_ctx, maker, src, precision):
+    """A field swept by one CTA and the same field swept by the grid-wide
+    launch give identical bits (same arithmetic, same schedule)."""
+    from gproshan_gb300 import _capi, meshgen
+    m = dev_mesh(gpu_ctx, *maker(meshgen))
+    dt = np.float64 if precision else np.float32
+    a, _, sa = _capi.ptp(m, src, dtype=dt, opts=_capi.make_opts(precision, local_window=1 << 30))
+    b, _, sb = _capi.ptp(m, src, dtype=dt, opts=_capi.make_opts(precision, local_window=1))
+    assert sa.n_iter == sb.n_iter and sa.relaxations == sb.relaxations
+    assert np.array_equal(a, b)

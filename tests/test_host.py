@@ -1,0 +1,96 @@
+"""Host-side checks that need no GPU: the C-ABI library builds and exports
+every symbol of include/gp_ptp.h, the host CHE builder matches the reference,
+and the GPU entry points fail loudly (no CPU fallback) when no GPU is there."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, ROOT
+
+CASES = golden_cases()
+
+
+def header_symbols():
+    txt = open(os.path.join(ROOT, "include", "gp_ptp.h")).read()
+    txt = re.sub(r"/\*.*?\*/", "", txt, flags=re.S)
+    return sorted(set(re.findall(r"\b(gp_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol(built_lib):
+    syms = header_symbols()
+    assert len(syms) >= 14
+    L = ctypes.CDLL(built_lib)
+    for s in syms:
+        assert hasattr(L, s), s
+    from gproshan_gb300 import _capi
+    assert set(_capi.SIGNATURES) == set(syms)
+
+
+def test_library_is_built_for_sm103a(built_lib):
+    import subprocess
+    r = subprocess.run(["cuobjdump", "--list-elf", built_lib], capture_output=True, text=True)
+    if r.returncode != 0:
+        pytest.skip("cuobjdump unavailable")
+    assert "sm_103a" in r.stdout
+
+
+@pytest.mark.parametrize("name,g", CASES, ids=[c[0] for c in CASES])
+def test_che_build_matches_reference(built_lib, name, g):
+    from gproshan_gb300 import _capi
+    OT, EVT, manifold = _capi.che_build(len(g["xyz"]), g["tri"])
+    assert np.array_equal(OT, g["OT"])
+    assert np.array_equal(EVT, g["EVT"])
+    assert manifold == (not (g["EVT"] == 0xFFFFFFFF).any() or name != "nonmanifold")
+
+
+def test_che_build_rejects_bad_index(built_lib):
+    from gproshan_gb300 import _capi
+    with pytest.raises(_capi.GPError):
+        _capi.che_build(3, np.array([[0, 1, 5]], np.uint32))
+
+
+def test_che_class_star_and_link(built_lib):
+    from gproshan_gb300 import che, meshgen
+    xyz, tri = meshgen.height_field(6, 0)
+    m = che(xyz, tri)
+    assert m.n_vertices() == 36 and m.n_faces() == 50
+    # interior vertex of a grid triangulated with one diagonal per cell has 6 neighbours
+    v = 2 * 6 + 2
+    assert len(m.star(v)) == 6 and len(m.link(v)) == 6
+    # corner: open fan, link has one more entry than the star
+    assert len(m.link(0)) == len(m.star(0)) + 1
+
+
+def test_meshgen_sizes():
+    from gproshan_gb300 import meshgen
+    xyz, tri = meshgen.icosphere(4, 0.1, 0)
+    assert len(xyz) == 10 * 4 ** 4 + 2 and len(tri) == 20 * 4 ** 4
+    assert np.allclose(np.linalg.norm(xyz, axis=1), 1.0)
+    xyz, tri = meshgen.height_field(64, 0)
+    assert len(xyz) == 64 * 64 and len(tri) == 2 * 63 * 63
+    xyz, tri = meshgen.torus(40, 25)
+    assert len(xyz) == 1000 and len(tri) == 2000
+
+
+def test_no_gpu_fails_loudly(built_lib):
+    """Without a usable GB300 the product path raises; it never computes on the CPU."""
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    from gproshan_gb300 import _capi, che, geodesics, meshgen
+    with pytest.raises(_capi.GPError) as e:
+        _capi.Context(0)
+    assert e.value.status == 6  # GP_ERR_NO_DEVICE
+    xyz, tri = meshgen.icosphere(2, 0.0, 0)
+    with pytest.raises(_capi.GPError):
+        geodesics(che(xyz, tri), [0], geodesics.PTP_GPU)
+
+
+def test_unsupported_options_raise(built_lib):
+    from gproshan_gb300 import che, geodesics, meshgen
+    xyz, tri = meshgen.icosphere(1, 0.0, 0)
+    with pytest.raises(NotImplementedError):
+        geodesics(che(xyz, tri), [0], geodesics.FM)
