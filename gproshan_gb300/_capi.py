@@ -41,12 +41,23 @@ class GPError(RuntimeError):
 class gp_ptp_opts(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("max_iter", C.c_uint32), ("tol", C.c_double),
                 ("threads", C.c_uint32), ("ctas", C.c_uint32), ("local_window", C.c_uint32),
-                ("reserved", C.c_uint32 * 3)]
+                ("round_coords", C.c_uint32), ("reserved", C.c_uint32 * 2)]
 
 
 class gp_ptp_stats(C.Structure):
     _fields_ = [("n_iter", C.c_uint32), ("n_limits", C.c_uint32), ("relaxations", C.c_uint64),
                 ("seconds", C.c_double)]
+
+
+class gp_call_stats(C.Structure):
+    _fields_ = [("launches", C.c_uint32), ("n_fields", C.c_uint32), ("fields_grid", C.c_uint32),
+                ("sweeps_grid", C.c_uint32), ("ms_toplesets", C.c_double), ("ms_renumber", C.c_double),
+                ("ms_local", C.c_double), ("ms_grid", C.c_double), ("ms_gather", C.c_double),
+                ("relax_local", C.c_uint64), ("relax_grid", C.c_uint64), ("h2d_bytes", C.c_uint64),
+                ("d2h_bytes", C.c_uint64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
 
 
 class gp_field(C.Structure):
@@ -78,6 +89,8 @@ SIGNATURES = {
     "gp_ptp_batch": (C.c_int, [C.c_void_p, C.POINTER(gp_field), C.c_uint32, C.POINTER(gp_ptp_opts),
                                C.c_int, C.c_uint32, C.POINTER(C.c_double)]),
     "gp_normalize_ptp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64]),
+    "gp_ctx_call_stats": (C.c_int, [C.c_void_p, C.POINTER(gp_call_stats)]),
+    "gp_ctx_step_trace": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32)]),
     "gp_fps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64,
                          C.c_double, C.POINTER(gp_ptp_opts), _u32p, C.POINTER(C.c_double),
                          C.POINTER(C.c_double)]),
@@ -157,6 +170,30 @@ class Context:
     def workspace_bytes(self) -> int:
         return int(lib().gp_ctx_workspace_bytes(self._h))
 
+    def call_stats(self) -> gp_call_stats:
+        cs = gp_call_stats()
+        self.check(lib().gp_ctx_call_stats(self._h, C.byref(cs)), "gp_ctx_call_stats")
+        return cs
+
+    def arm_step_trace(self, cap: int):
+        self.check(lib().gp_ctx_step_trace(self._h, cap, None, None), "gp_ctx_step_trace")
+        self._trace_cap = cap
+
+    def step_trace(self):
+        """(t_ns, tiles, live) per step of the last call's grid launch."""
+        cap = getattr(self, "_trace_cap", 0)
+        out = np.zeros(2 * max(cap, 1), np.uint64)
+        n = C.c_uint32(0)
+        self.check(lib().gp_ctx_step_trace(self._h, cap, out.ctypes.data_as(C.c_void_p), C.byref(n)),
+                   "gp_ctx_step_trace")
+        w = out[:2 * n.value].reshape(-1, 2)
+        return w[:, 0].astype(np.int64), (w[:, 1] >> np.uint64(32)).astype(np.int64), \
+            (w[:, 1] & np.uint64(0xffffffff)).astype(np.int64)
+
+    @property
+    def stream(self) -> int:
+        return int(lib().gp_ctx_stream(self._h) or 0)
+
     def close(self):
         if self._h:
             lib().gp_ctx_destroy(self._h)
@@ -226,8 +263,9 @@ def toplesets(mesh: DeviceMesh, sources):
 
 
 def make_opts(precision: int = GP_F32, max_iter: int = 0, tol: float = 0.0, ctas: int = 0,
-              local_window: int = 0) -> gp_ptp_opts:
+              local_window: int = 0, round_coords: bool = False) -> gp_ptp_opts:
     o = gp_ptp_opts()
+    o.round_coords = int(bool(round_coords))
     o.precision = precision
     o.max_iter = max_iter
     o.tol = tol
@@ -259,7 +297,7 @@ def ptp(mesh: DeviceMesh, sources, limits=None, sorted_=None, dtype=np.float32, 
 
 
 def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP_F32, ctas: int = 0,
-              with_stats: bool = True, local_window: int = 0):
+              with_stats: bool = True, local_window: int = 0, round_coords: bool = False):
     """Solve many fields together (host arrays).  Returns (dists, stats, seconds)."""
     n = len(sources_list)
     out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
@@ -279,7 +317,7 @@ def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP
         fields[k].clusters = None
         fields[k].stats = C.addressof(stats[k]) if with_stats else None
     sec = C.c_double(0)
-    opts = make_opts(precision, ctas=ctas, local_window=local_window)
+    opts = make_opts(precision, ctas=ctas, local_window=local_window, round_coords=round_coords)
     st = lib().gp_ptp_batch(ctx.handle, fields, n, C.byref(opts), out_t, 0, C.byref(sec))
     ctx.check(st, "gp_ptp_batch")
     return dists, stats, sec.value

@@ -29,7 +29,11 @@ int ptp_local_max_ctas(int device, bool f64, bool clusters);
 cudaError_t launch_classify(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
                             cudaStream_t s);
 cudaError_t launch_ptp_local(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
-                             uint32_t ctas, bool f64, bool clusters, cudaStream_t s);
+                             uint32_t ctas, uint32_t local_window, bool f64, bool clusters, cudaStream_t s);
+cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
+                       uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
+                       cudaStream_t s);
+uint32_t ptp_grid_max_fields();
 } // namespace gp
 
 using namespace gp;
@@ -44,9 +48,14 @@ struct gp_ctx {
 	void *pin = nullptr;       // grow-only pinned host staging
 	size_t pin_bytes = 0;
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+	cudaEvent_t ph[6] = {};    // phase boundaries of the last call
+	gp_call_stats last{};
+	unsigned long long *steps = nullptr;   // grid-launch step trace (device), if enabled
+	uint32_t steps_cap = 0;
 	int bfs_ctas = 0;
 	int ptp_ctas[4] = {0, 0, 0, 0};
 	int local_ctas[4] = {0, 0, 0, 0};
+	uint32_t grid_ctas = 0;    // CTAs of the last grid launch
 };
 
 struct gp_mesh {
@@ -57,6 +66,13 @@ struct gp_mesh {
 };
 
 namespace {
+
+// kernels launched by launch_scan_u32 for n elements
+uint32_t scan_launches(size_t n)
+{
+	const size_t tile = 1024;
+	return n <= tile ? 1u : 2u + scan_launches((n + tile - 1) / tile);
+}
 
 void set_err(gp_ctx *ctx, const char *fmt, ...)
 {
@@ -181,7 +197,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const bool f64 = o.precision == GP_F64;
 	const bool clusters = stage == Stage::ptp && std::any_of(reqs, reqs + F, [](const Req &r) { return r.clusters; });
 	const bool given_tops = reqs[0].limits != nullptr;
-	const size_t tsz = f64 ? sizeof(double) : sizeof(float);
+	const size_t tsz = 8;  // double (FP64 path) or a (hi, lo) float pair (FP32 path)
 	const size_t osz = out_type == GP_F64 ? sizeof(double) : sizeof(float);
 	const uint32_t NTH = (uint32_t) ptp_threads();
 
@@ -263,6 +279,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_act = cv.add<uint32_t>(F), o_ts = cv.add<uint32_t>(F + 1), o_aux = cv.add<uint32_t>(tiles + 2);
 	const size_t o_sync = cv.add<GridSync>(2), o_base = cv.add<uint32_t>(F + 1), o_vbase = cv.add<uint32_t>(F + 1);
 	const size_t o_queue = cv.add<uint32_t>(4);
+	const size_t o_notok = cv.add<uint32_t>(3 * (size_t) F), o_bar = cv.add<uint32_t>(4);
 	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
 	const size_t o_sorted = cv.add<uint32_t>(tot), o_lim = cv.add<uint32_t>(tot), o_inv = cv.add<uint32_t>(tot);
 	size_t o_cnt = 0, o_scan = 0, o_P = 0, o_Pd = 0, o_off = 0, o_fan = 0, o_D0 = 0, o_D1 = 0, o_C0 = 0, o_C1 = 0;
@@ -331,6 +348,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			d.dist_out = out_dev ? r.dist : P(o_out) + (size_t) vbase[f] * osz;
 			d.out_f64 = out_type == GP_F64;
 			d.max_iter = o.max_iter;
+			d.round_coords = o.round_coords ? 1u : 0u;
 			d.tol = o.tol > 0 ? o.tol : GP_PTP_TOL;
 		}
 		if(given_tops) hs[f].n_limits = r.nl;
@@ -387,6 +405,10 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	hp.tile_aux = reinterpret_cast<uint32_t *>(P(o_aux));
 	hp.cap_tiles = (uint32_t) tiles;
 	GP_CUDA(ctx, cudaMemcpyAsync(P(o_plan), &hp, sizeof(hp), cudaMemcpyHostToDevice, s));
+	uint64_t h2d = po + sizeof(hp), d2h = 0;
+	if(clusters && !out_dev)
+		for(uint32_t f = 0; f < F; f++)
+			if(reqs[f].clusters) h2d += 4ull * reqs[f].mesh->nv;
 	GP_CUDA(ctx, cudaStreamSynchronize(s));  // hp lives on this stack frame
 
 	FieldDev *dF = reinterpret_cast<FieldDev *>(P(o_fields));
@@ -398,32 +420,52 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 
 	// ---- device work ---------------------------------------------------------
 	GP_CUDA(ctx, cudaMemsetAsync(dSync, 0, 2 * sizeof(GridSync), s));
+	gp_call_stats cs{};
+	cs.n_fields = F;
 	GP_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
+	GP_CUDA(ctx, cudaEventRecord(ctx->ph[0], s));
 	if(!given_tops)
 	{
 		GP_CUDA(ctx, launch_bfs_setup(dF, dS, dVbase, F, (uint32_t) vtot, s));
 		GP_CUDA(ctx, launch_toplesets(dF, dS, F, &dSync->count, (uint32_t) ctx->bfs_ctas, s));
+		cs.launches += (vtot ? 1 : 0) + 2;
 	}
+	GP_CUDA(ctx, cudaEventRecord(ctx->ph[1], s));
 	if(stage == Stage::ptp)
 	{
 		GP_CUDA(ctx, launch_renumber_batch(dF, dS, dBase, F, (uint32_t) tot, reinterpret_cast<uint32_t *>(P(o_cnt)),
 		                                   reinterpret_cast<uint32_t *>(P(o_scan)), f64, clusters, s));
+		cs.launches += 4 + scan_launches(tot);
+		GP_CUDA(ctx, cudaEventRecord(ctx->ph[2], s));
 		const int kv = (f64 ? 2 : 0) + (clusters ? 1 : 0);
 		const uint32_t lw = o.local_window ? o.local_window : 4096u;
 		GP_CUDA(ctx, launch_classify(dF, dS, F, lw, s));
 		GP_CUDA(ctx, launch_ptp_local(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_queue)),
-		                              (uint32_t) ctx->local_ctas[kv], f64, clusters, s));
-		const int maxc = ctx->ptp_ctas[kv];
+		                              (uint32_t) ctx->local_ctas[kv], lw, f64, clusters, s));
+		GP_CUDA(ctx, cudaEventRecord(ctx->ph[3], s));
+		const int maxc = ptp_max_ctas(ctx->device, f64, clusters, F);
 		uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
-		GP_CUDA(ctx, launch_ptp(dF, dS, F, dP, dSync + 1, ctas, f64, clusters, s));
+		ctx->grid_ctas = ctas;
+		GP_CUDA(ctx, launch_ptp(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_notok)),
+		                        reinterpret_cast<uint32_t *>(P(o_bar)), ctas, f64, clusters, ctx->steps,
+		                        ctx->steps_cap, s));
+		GP_CUDA(ctx, cudaEventRecord(ctx->ph[4], s));
 		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s));
+		cs.launches += 4;
 	}
+	else
+		for(int k = 2; k < 5; k++) GP_CUDA(ctx, cudaEventRecord(ctx->ph[k], s));
+	GP_CUDA(ctx, cudaEventRecord(ctx->ph[5], s));
 	GP_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
 
 	// ---- downloads -------------------------------------------------------------
 	GridSync hsync[2];
 	GP_CUDA(ctx, cudaMemcpyAsync(hsync, dSync, sizeof(hsync), cudaMemcpyDeviceToHost, s));
 	GP_CUDA(ctx, cudaMemcpyAsync(hs.data(), dS, sizeof(FieldState) * F, cudaMemcpyDeviceToHost, s));
+	d2h += sizeof(hsync) + sizeof(FieldState) * F;
+	if(stage == Stage::ptp && !out_dev)
+		for(uint32_t f = 0; f < F; f++)
+			d2h += (uint64_t) reqs[f].mesh->nv * (osz + (reqs[f].clusters ? 4 : 0));
 	if(stage == Stage::ptp && !out_dev)
 		for(uint32_t f = 0; f < F; f++)
 		{
@@ -437,11 +479,42 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	GP_CUDA(ctx, cudaStreamSynchronize(s));
 	uint32_t ferr = 0;
 	for(uint32_t f = 0; f < F; f++) ferr |= hs[f].status;
+	if(stage == Stage::ptp)
+	{
+		uint32_t gb[4];
+		GP_CUDA(ctx, cudaMemcpy(gb, P(o_bar), sizeof(gb), cudaMemcpyDeviceToHost));
+		ferr |= gb[2];
+	}
 	st = map_dev_err(ctx, hsync[0].err | hsync[1].err | ferr, stage == Stage::ptp ? "ptp" : "toplesets");
 	if(st != GP_OK) return st;
 	float ms = 0.f;
 	GP_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
 	if(seconds) *seconds = ms * 1e-3;
+	{
+		float pm[5];
+		for(int k = 0; k < 5; k++) GP_CUDA(ctx, cudaEventElapsedTime(&pm[k], ctx->ph[k], ctx->ph[k + 1]));
+		cs.ms_toplesets = pm[0];
+		cs.ms_renumber = pm[1];
+		cs.ms_local = pm[2];
+		cs.ms_grid = pm[3];
+		cs.ms_gather = pm[4];
+		for(uint32_t f = 0; f < F; f++)
+		{
+			if(hs[f].big)
+			{
+				cs.fields_grid++;
+				cs.relax_grid += hs[f].relax;
+			}
+			else cs.relax_local += hs[f].relax;
+		}
+		uint32_t hbar[4] = {0, 0, 0, 0};
+		if(stage == Stage::ptp)
+			GP_CUDA(ctx, cudaMemcpy(hbar, P(o_bar), sizeof(hbar), cudaMemcpyDeviceToHost));
+		cs.sweeps_grid = ctx->grid_ctas ? hbar[0] / ctx->grid_ctas : 0;
+		cs.h2d_bytes = h2d;
+		cs.d2h_bytes = d2h + (stage == Stage::ptp ? 2 * sizeof(hbar) : 0);
+		ctx->last = cs;
+	}
 	for(uint32_t f = 0; f < F; f++)
 		if(reqs[f].stats)
 		{
@@ -523,10 +596,12 @@ gp_status gp_ctx_create(int device, gp_ctx **out)
 	ctx->bfs_ctas = toplesets_max_ctas(device);
 	for(int k = 0; k < 4; k++)
 	{
-		ctx->ptp_ctas[k] = ptp_max_ctas(device, k >= 2, k & 1);
+		ctx->ptp_ctas[k] = ptp_max_ctas(device, k >= 2, k & 1, 1);
 		ctx->local_ctas[k] = ptp_local_max_ctas(device, k >= 2, k & 1);
 	}
-	if(ctx->bfs_ctas <= 0 || ctx->ptp_ctas[0] <= 0)
+	for(int k = 0; k < 6; k++)
+		if(cudaEventCreate(&ctx->ph[k]) != cudaSuccess) ctx->ph[k] = nullptr;
+	if(ctx->bfs_ctas <= 0 || ctx->ptp_ctas[0] <= 0 || !ctx->ph[5])
 	{
 		cudaGetLastError();
 		gp_ctx_destroy(ctx);
@@ -543,13 +618,48 @@ void gp_ctx_destroy(gp_ctx *ctx)
 	if(ctx->stream) cudaStreamSynchronize(ctx->stream);
 	if(ctx->ws) cudaFree(ctx->ws);
 	if(ctx->pin) cudaFreeHost(ctx->pin);
+	if(ctx->steps) cudaFree(ctx->steps);
 	if(ctx->ev0) cudaEventDestroy(ctx->ev0);
 	if(ctx->ev1) cudaEventDestroy(ctx->ev1);
+	for(int k = 0; k < 6; k++)
+		if(ctx->ph[k]) cudaEventDestroy(ctx->ph[k]);
 	if(ctx->stream) cudaStreamDestroy(ctx->stream);
 	delete ctx;
 }
 
 const char *gp_ctx_last_error(const gp_ctx *ctx) { return ctx ? ctx->err.c_str() : "null context"; }
+
+gp_status gp_ctx_step_trace(gp_ctx *ctx, uint32_t cap, uint64_t *out, uint32_t *n_out)
+{
+	if(!ctx) return GP_ERR_INVALID_ARG;
+	if(!out)
+	{
+		// (re)arm: record up to cap steps of the following calls' grid launches
+		if(ctx->steps) cudaFree(ctx->steps);
+		ctx->steps = nullptr;
+		ctx->steps_cap = 0;
+		if(cap)
+		{
+			GP_CUDA(ctx, cudaMalloc(&ctx->steps, 16 * (size_t) cap));
+			ctx->steps_cap = cap;
+		}
+		return GP_OK;
+	}
+	if(!ctx->steps || !n_out) return GP_ERR_INVALID_ARG;
+	const uint32_t n = std::min(cap, ctx->steps_cap);
+	GP_CUDA(ctx, cudaMemcpy(out, ctx->steps, 16 * (size_t) n, cudaMemcpyDeviceToHost));
+	uint32_t k = 0;
+	while(k < n && out[2 * k]) k++;
+	*n_out = k;
+	return GP_OK;
+}
+
+gp_status gp_ctx_call_stats(const gp_ctx *ctx, gp_call_stats *out)
+{
+	if(!ctx || !out) return GP_ERR_INVALID_ARG;
+	*out = ctx->last;
+	return GP_OK;
+}
 void *gp_ctx_stream(gp_ctx *ctx) { return ctx ? (void *) ctx->stream : nullptr; }
 size_t gp_ctx_workspace_bytes(const gp_ctx *ctx) { return ctx ? ctx->ws_bytes : 0; }
 
@@ -761,7 +871,18 @@ gp_status gp_ptp_batch(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, c
 		reqs[f] = Req{fields[f].mesh, fields[f].sources, fields[f].n_sources, nullptr, 0, nullptr,
 		              fields[f].dist, fields[f].clusters, fields[f].stats};
 	const bool dev = (flags & GP_BATCH_DEVICE_POINTERS) != 0;
-	return run(ctx, reqs.data(), n_fields, opts, dist_type, dev, dev, Stage::ptp, nullptr, seconds);
+	const uint32_t chunk = ptp_grid_max_fields();
+	double total = 0;
+	for(uint32_t f0 = 0; f0 < n_fields; f0 += chunk)
+	{
+		double sec = 0;
+		const gp_status st = run(ctx, reqs.data() + f0, std::min(chunk, n_fields - f0), opts, dist_type, dev, dev,
+		                         Stage::ptp, nullptr, &sec);
+		if(st != GP_OK) return st;
+		total += sec;
+	}
+	if(seconds) *seconds = total;
+	return GP_OK;
 }
 
 gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n)

@@ -70,7 +70,7 @@ struct FieldDev {
 	uint32_t trace_cap;
 	uint32_t out_f64;         // 1: dist_out is double
 	uint32_t max_iter;        // 0: 2 * n_limits
-	uint32_t pad;
+	uint32_t round_coords;    // FP64 path on the float-rounded coordinates
 	double tol;
 };
 
@@ -124,9 +124,7 @@ cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fie
 int toplesets_max_ctas(int device);
 
 // gp_ptp.cu
-cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, PlanDev *plan,
-                       GridSync *sync, uint32_t ctas, bool f64, bool clusters, cudaStream_t s);
-int ptp_max_ctas(int device, bool f64, bool clusters);
+int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields);
 cudaError_t launch_argmax_abs(const void *dist, bool f64, uint32_t n, unsigned long long *out,
                               cudaStream_t s);
 

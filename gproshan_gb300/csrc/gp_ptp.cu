@@ -18,6 +18,7 @@
 // rule to each field and lays out the next step's tiles.  No host round trip.
 #include <cfloat>
 #include <cmath>
+#include <type_traits>
 
 #include "gp_common.cuh"
 
@@ -25,7 +26,7 @@ namespace gp {
 
 namespace {
 
-constexpr int NT = 512;  // threads of a grid-launch CTA (one tile = NT window vertices)
+constexpr int NT = 256;  // threads of a grid-launch CTA (one tile = NT window vertices)
 
 // Distance/label load: coherent (L2) when other CTAs of the launch write the
 // buffer, plain otherwise.
@@ -59,19 +60,21 @@ struct Nb32 {
 	uint32_t u;
 };
 
-template <bool COH>
-__device__ __forceinline__ Nb32 load_nb32(const float4 *__restrict__ P, const float *D, uint32_t u, float4 pv)
+// sqrt and reciprocal to about 1 ulp on the SFU (PTX .approx forms).  Used on
+// edge-sized offsets only: their error is ~1e-7 of an edge length, far below
+// the solver's own rounding on the distances.
+__device__ __forceinline__ float sqrt_a(float x)
 {
-	Nb32 n;
-	const float4 pu = __ldg(P + u);
-	n.x = pu.x - pv.x;
-	n.y = pu.y - pv.y;
-	n.z = pu.z - pv.z;
-	n.t = ld_d<float, COH>(D + u);
-	n.q = fmaf(n.x, n.x, fmaf(n.y, n.y, n.z * n.z));
-	n.l = sqrtf(n.q);
-	n.u = u;
-	return n;
+	float y;
+	asm("sqrt.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
+}
+
+__device__ __forceinline__ float rcp_a(float x)
+{
+	float y;
+	asm("rcp.approx.f32 %0, %1;" : "=f"(y) : "f"(x));
+	return y;
 }
 
 __device__ __forceinline__ float update32(const Nb32 &a, const Nb32 &b)
@@ -85,15 +88,16 @@ __device__ __forceinline__ float update32(const Nb32 &a, const Nb32 &b)
 	const float cx = fmaf(a.y, b.z, -a.z * b.y);
 	const float cy = fmaf(a.z, b.x, -a.x * b.z);
 	const float cz = fmaf(a.x, b.y, -a.y * b.x);
-	const float A = sqrtf(fmaf(cx, cx, fmaf(cy, cy, cz * cz)));
-	if(!(A > 0.f)) return NAN;
+	const float A2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+	if(!(A2 > 0.f)) return NAN;
 	const float dt = b.t - a.t;
 	const float r = fmaf(-dt, dt, e2);
 	if(r < 0.f) return fb;
 	const float a1 = -fmaf(a.x, ex, fmaf(a.y, ey, a.z * ez));
 	const float a0 = fmaf(b.x, ex, fmaf(b.y, ey, b.z * ez));
 	const float q01 = fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z));
-	const float delta = fmaf(a1, dt, A * sqrtf(r)) / e2;
+	// A*sqrt(r) = sqrt(A^2 r): one root per triangle
+	const float delta = fmaf(a1, dt, sqrt_a(A2 * r)) * rcp_a(e2);
 	if(fmaf(a0, delta, q01 * dt) > 0.f && fmaf(a1, delta, -a.q * dt) > 0.f)
 		return a.t + delta;
 	return fb;
@@ -173,41 +177,21 @@ __device__ __forceinline__ double update64(const Nb64 &A0, const Nb64 &A1)
 // ---------------------------------------------------------------------------
 // Relaxation of one vertex: new = min(old[v], min over star triangles).
 // ---------------------------------------------------------------------------
+// Fan entries whose loads are issued together before any update is computed:
+// a vertex of valence <= FB costs three dependent memory trips (offset, fan
+// indices, neighbour positions + distances) instead of two per neighbour.
+constexpr uint32_t FB = 8;
+
 template <bool CL, bool COH>
-__device__ __forceinline__ float relax32(const FieldDev &F, uint32_t v, const float *Do, const uint32_t *Co,
-                                         uint32_t &lab)
+__device__ __forceinline__ void take32(const Nb32 &a, const Nb32 &b, float &best, uint32_t &lab, const uint32_t *Co)
 {
-	const uint32_t o0f = __ldg(F.off + v);
-	const uint32_t o1 = __ldg(F.off + v + 1) & FAN_MASK;
-	const uint32_t o0 = o0f & FAN_MASK;
-	float best = ld_d<float, COH>(Do + v);
-	if(CL) lab = ld_d<uint32_t, COH>(Co + v);
-	if(o1 <= o0) return best;
-	const float4 pv = __ldg(F.P + v);
-	const uint32_t *fan = F.fan;
-	const Nb32 first = load_nb32<COH>(F.P, Do, __ldg(fan + o0), pv);
-	Nb32 prev = first;
-	for(uint32_t e = o0 + 1; e < o1; e++)
+	const float p = update32(a, b);
+	if(p < best)
 	{
-		const Nb32 cur = load_nb32<COH>(F.P, Do, __ldg(fan + e), pv);
-		const float p = update32(prev, cur);
-		if(p < best)
-		{
-			best = p;
-			if(CL) lab = cur.t < prev.t ? ld_d<uint32_t, COH>(Co + cur.u) : ld_d<uint32_t, COH>(Co + prev.u);
-		}
-		prev = cur;
+		best = p;
+		// GPU label rule (src/cuda/geodesics_ptp.cu:277): a = x0 (next), b = x1 (prev)
+		if(CL) lab = b.t < a.t ? ld_d<uint32_t, COH>(Co + b.u) : ld_d<uint32_t, COH>(Co + a.u);
 	}
-	if(o0f & FAN_CLOSED)
-	{
-		const float p = update32(prev, first);
-		if(p < best)
-		{
-			best = p;
-			if(CL) lab = first.t < prev.t ? ld_d<uint32_t, COH>(Co + first.u) : ld_d<uint32_t, COH>(Co + prev.u);
-		}
-	}
-	return best;
 }
 
 template <bool CL, bool COH>
@@ -247,18 +231,10 @@ __device__ __forceinline__ double relax64(const FieldDev &F, uint32_t v, const d
 	return best;
 }
 
-struct PtpArgs {
-	FieldDev *fields;
-	FieldState *state;
-	uint32_t n_fields;
-	PlanDev *plan;
-	GridSync *sync;
-};
-
 // Open the next sweep if the reference loop would run one
 // (`while(i < j && iter++ < max_iter)` then the K/2 band,
 // src/cuda/geodesics_ptp.cu:206-212), else retire the field.
-__device__ __forceinline__ void open_sweep(const FieldDev &F, FieldState &st)
+__device__ __forceinline__ void open_sweep(const FieldDev &F, FieldState &st, bool trace)
 {
 	if(st.i < st.j && st.iter < st.max_iter)
 	{
@@ -268,13 +244,135 @@ __device__ __forceinline__ void open_sweep(const FieldDev &F, FieldState &st)
 		st.win_e = F.limits[st.j];
 		st.chk_e = F.limits[st.i + 1];
 		st.live = 1;
-		if(F.trace && st.n_iter < F.trace_cap)
+		if(trace && F.trace && st.n_iter < F.trace_cap)
 		{
 			F.trace[2 * st.n_iter] = st.i;
 			F.trace[2 * st.n_iter + 1] = st.j;
 		}
 	}
 	else st.live = 0;
+}
+
+// The schedule rule applied after every sweep (src/cuda/geodesics_ptp.cu:224-228).
+__device__ __forceinline__ void close_sweep(FieldState &st, bool converged)
+{
+	st.relax += st.win_e - st.win_s;
+	if(converged) st.i++;
+	if(st.j < st.n_limits - 1) st.j++;
+	st.d ^= 1u;
+	st.n_iter++;
+}
+
+// ---------------------------------------------------------------------------
+// FP32 path storage: distances are double-float pairs (hi, lo).  A vertex is
+// relaxed on distances RELATIVE to a base (its own distance, or while it is
+// still INF its smallest loaded neighbour's), so the FP32 solver only sees
+// edge-sized offsets and rounds to ~1e-7 of an edge instead of ~1e-7 of the
+// distance; the new value is base + best offset, formed exactly in
+// double-float.  This keeps the ring-i test (relative change < tol) on the
+// same side of the threshold as an FP64 run, sweep after sweep.
+// ---------------------------------------------------------------------------
+template <bool COH>
+__device__ __forceinline__ float2 ld2(const float2 *p)
+{
+	if constexpr(COH) return __ldcg(p);
+	else return *p;
+}
+
+__device__ __forceinline__ float rel_to(float2 dv, float bh, float bl)
+{
+	return dv.x == INFINITY ? INFINITY : (dv.x - bh) + (dv.y - bl);
+}
+
+__device__ __forceinline__ Nb32 make_nb(float4 pu, float t, float4 pv, uint32_t u)
+{
+	Nb32 n;
+	n.x = pu.x - pv.x;
+	n.y = pu.y - pv.y;
+	n.z = pu.z - pv.z;
+	n.t = t;
+	n.q = fmaf(n.x, n.x, fmaf(n.y, n.y, n.z * n.z));
+	n.l = sqrt_a(n.q);
+	n.u = u;
+	return n;
+}
+
+// Relaxation of one vertex on the FP32 path: new = min(old, star updates),
+// with the strict `if(p < best)` order of the reference (relax_ptp,
+// src/cuda/geodesics_ptp.cu:234-282).  All fan indices of a vertex of valence
+// <= FB are fetched at once, the neighbours in chunks of FC (bounded
+// registers, several loads in flight).  Returns the new (hi, lo) pair.
+constexpr uint32_t FC = 4;
+
+template <bool CL, bool COH>
+__device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const float2 *Do, const uint32_t *Co,
+                                          uint32_t &lab)
+{
+	const uint32_t o0f = __ldg(F.off + v);
+	const uint32_t o1 = __ldg(F.off + v + 1) & FAN_MASK;
+	const uint32_t o0 = o0f & FAN_MASK;
+	const float2 vd = ld2<COH>(Do + v);
+	if(CL) lab = ld_d<uint32_t, COH>(Co + v);
+	if(o1 <= o0) return vd;
+	const uint32_t n = o1 - o0;
+	const float4 pv = __ldg(F.P + v);
+	const uint32_t *fan = F.fan + o0;
+	uint32_t u[FB];
+#pragma unroll
+	for(uint32_t k = 0; k < FB; k++) u[k] = k < n ? __ldg(fan + k) : 0u;
+	// base of the relative distances: the vertex itself, or (while it is INF)
+	// its smallest neighbour among the first FB
+	float bh = vd.x, bl = vd.y;
+	if(bh == INFINITY)
+	{
+		float m = INFINITY;
+#pragma unroll
+		for(uint32_t k = 0; k < FB; k++)
+			if(k < n) m = fminf(m, ld2<COH>(Do + u[k]).x);
+		bh = m == INFINITY ? 0.f : m;
+		bl = 0.f;
+	}
+	const float old_rel = vd.x == INFINITY ? INFINITY : 0.f;
+	float best = old_rel;
+	Nb32 first, last;
+#pragma unroll
+	for(uint32_t c = 0; c < FB; c += FC)
+	{
+		float4 pk[FC];
+		float2 dk[FC];
+#pragma unroll
+		for(uint32_t q = 0; q < FC; q++)
+			if(c + q < n)
+			{
+				pk[q] = __ldg(F.P + u[c + q]);
+				dk[q] = ld2<COH>(Do + u[c + q]);
+			}
+#pragma unroll
+		for(uint32_t q = 0; q < FC; q++)
+			if(c + q < n)
+			{
+				const Nb32 cur = make_nb(pk[q], rel_to(dk[q], bh, bl), pv, u[c + q]);
+				if(c + q == 0) first = cur;
+				else take32<CL, COH>(last, cur, best, lab, Co);
+				last = cur;
+			}
+	}
+	// valence above FB: the rest one neighbour at a time
+	for(uint32_t e = FB; e < n; e++)
+	{
+		const uint32_t w = __ldg(fan + e);
+		const Nb32 cur = make_nb(__ldg(F.P + w), rel_to(ld2<COH>(Do + w), bh, bl), pv, w);
+		take32<CL, COH>(last, cur, best, lab, Co);
+		last = cur;
+	}
+	if(o0f & FAN_CLOSED) take32<CL, COH>(last, first, best, lab, Co);
+	if(!(best < old_rel)) return vd;
+	// (bh, bl) + best, exactly in double-float
+	const float s0 = bh + best;
+	const float bb = s0 - bh;
+	const float e = (bh - (s0 - bb)) + (best - bb) + bl;
+	const float h = s0 + e;
+	return make_float2(h, e - (h - s0));
 }
 
 // Relax window vertex v of field F (buffers d -> d^1) and, if v is in the
@@ -284,29 +382,40 @@ __device__ __forceinline__ void open_sweep(const FieldDev &F, FieldState &st)
 template <typename T, bool CL, bool COH>
 __device__ __forceinline__ int sweep_vertex(const FieldDev &F, uint32_t d, uint32_t v, uint32_t chk_e)
 {
-	const T *Do = static_cast<const T *>(F.D[d]);
-	T *Dn = static_cast<T *>(F.D[d ^ 1u]);
 	const uint32_t *Co = CL ? F.C[d] : nullptr;
 	uint32_t lab = 0;
-	T nv;
-	if constexpr(sizeof(T) == 4) nv = relax32<CL, COH>(F, v, reinterpret_cast<const float *>(Do), Co, lab);
-	else nv = relax64<CL, COH>(F, v, reinterpret_cast<const double *>(Do), Co, lab);
-	Dn[v] = nv;
-	if(CL) F.C[d ^ 1u][v] = lab;
-	if(v < chk_e)
+	double o, nd;
+	if constexpr(sizeof(T) == 4)
 	{
-		const double o = (double) ld_d<T, COH>(Do + v);
-		const double err = fabs((double) nv - o) / o;
-		return !(err < F.tol);
+		const float2 *Do = static_cast<const float2 *>(F.D[d]);
+		const float2 nv = relax32<CL, COH>(F, v, Do, Co, lab);
+		static_cast<float2 *>(F.D[d ^ 1u])[v] = nv;
+		if(v >= chk_e) goto labels;
+		const float2 ov = ld2<COH>(Do + v);
+		o = (double) ov.x + (double) ov.y;
+		nd = (double) nv.x + (double) nv.y;
 	}
+	else
+	{
+		const double *Do = static_cast<const double *>(F.D[d]);
+		const double nv = relax64<CL, COH>(F, v, Do, Co, lab);
+		static_cast<double *>(F.D[d ^ 1u])[v] = nv;
+		if(v >= chk_e) goto labels;
+		o = ld_d<double, COH>(Do + v);
+		nd = nv;
+	}
+	if(CL) F.C[d ^ 1u][v] = lab;
+	// relative_error + is_ok (src/cuda/geodesics_ptp.cu:284-299, 371-375), in FP64
+	return !(fabs(nd - o) / o < F.tol);
+labels:
+	if(CL) F.C[d ^ 1u][v] = lab;
 	return 0;
 }
 
 // ---------------------------------------------------------------------------
-// classify: per field, the largest window its schedule can open
-// (max over j of limits[j] - limits[j/2]) decides whether one CTA sweeps it
-// (ptp_local_kernel) or the whole grid (ptp_kernel).  Also resets the
-// schedule state so that fields with no sweep read back d = 0.
+// classify: reset every field's schedule state (i = 1, j = 2, d = 0) and
+// record the largest window its schedule could open, max_j limits[j] -
+// limits[j/2] (statistics).  Every field starts on one CTA.
 // ---------------------------------------------------------------------------
 __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window)
 {
@@ -321,7 +430,7 @@ __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 	if(lane == 0)
 	{
 		st.bound = bound;
-		st.big = nl >= 3 && bound > local_window;
+		st.big = 0;
 		st.nr = nl ? F.limits[nl - 1] : 0;
 		st.i = 1;
 		st.j = 2;
@@ -333,19 +442,22 @@ __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 		st.relax = 0;
 		st.max_iter = F.max_iter ? F.max_iter : (nl << 1);
 	}
+	(void) local_window;
 }
 
 // ---------------------------------------------------------------------------
-// One CTA sweeps one field from its first to its last sweep
-// (run_ptp_gpu's loop, src/cuda/geodesics_ptp.cu:198-229): the window is
-// swept in CTA-sized chunks, __syncthreads_or() both merges the ring-i test
-// and separates the sweeps.  Every thread keeps the schedule in registers.
+// One CTA sweeps one field (run_ptp_gpu's loop, src/cuda/geodesics_ptp.cu:
+// 198-229): the window is swept in CTA-sized chunks and __syncthreads_or()
+// both merges the ring-i test and separates the sweeps.  Every thread keeps
+// the schedule in registers.  When the next window would exceed
+// local_window vertices the field is handed, mid-schedule, to the grid-wide
+// launch (state saved with that sweep already opened, big = 1).
 // ---------------------------------------------------------------------------
 constexpr int LT = 512;
 
 template <typename T, bool CL>
 __global__ void __launch_bounds__(LT) ptp_local_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields,
-                                                       uint32_t *queue)
+                                                       uint32_t *queue, uint32_t local_window)
 {
 	__shared__ uint32_t s_f;
 	for(;;)
@@ -356,26 +468,21 @@ __global__ void __launch_bounds__(LT) ptp_local_kernel(FieldDev *fields, FieldSt
 		__syncthreads();
 		if(f >= n_fields) return;
 		FieldState &gst = state[f];
-		if(gst.big || gst.n_limits < 3) continue;
+		if(gst.n_limits < 3) continue;
 		const FieldDev &F = fields[f];
 		FieldState st = {};
 		st.i = 1;
 		st.j = 2;
 		st.max_iter = gst.max_iter;
-		const uint32_t nl = gst.n_limits;
-		open_sweep(F, st);
-		while(st.live)
+		st.n_limits = gst.n_limits;
+		open_sweep(F, st, threadIdx.x == 0);
+		while(st.live && st.win_e - st.win_s <= local_window)
 		{
 			int bad = 0;
 			for(uint32_t v = st.win_s + threadIdx.x; v < st.win_e; v += LT)
 				bad |= sweep_vertex<T, CL, false>(F, st.d, v, st.chk_e);
-			const int any = __syncthreads_or(bad);
-			st.relax += st.win_e - st.win_s;
-			if(!any) st.i++;
-			if(st.j < nl - 1) st.j++;
-			st.d ^= 1u;
-			st.n_iter++;
-			open_sweep(F, st);
+			close_sweep(st, !__syncthreads_or(bad));
+			open_sweep(F, st, threadIdx.x == 0);
 		}
 		if(threadIdx.x == 0)
 		{
@@ -385,139 +492,227 @@ __global__ void __launch_bounds__(LT) ptp_local_kernel(FieldDev *fields, FieldSt
 			gst.iter = st.iter;
 			gst.n_iter = st.n_iter;
 			gst.relax = st.relax;
+			gst.live = st.live;
+			gst.win_s = st.win_s;
+			gst.win_e = st.win_e;
+			gst.chk_e = st.chk_e;
+			gst.big = st.live;  // still running: the grid-wide launch continues it
 		}
 	}
 }
 
 // ---------------------------------------------------------------------------
-// Grid-wide persistent sweep of the big fields, all in lockstep: each step the
-// CTAs walk the tiles of every live window, and the last CTA at the barrier
-// applies the schedule rule to each field and lays out the next step.
+// Grid-wide persistent sweeps of the fields handed over by ptp_local_kernel,
+// all in lockstep.  Every CTA holds the schedule of every field in shared
+// memory and applies the reference's rule itself after each barrier (the
+// rule is deterministic, so all copies agree); the only cross-CTA data per
+// step are the ring-i flags, triple-buffered so that they can be cleared
+// without an extra barrier.  A step: walk the tiles of all live windows ->
+// counting barrier -> read the flags, advance, re-plan.
 // ---------------------------------------------------------------------------
+struct GridArgs {
+	FieldDev *fields;
+	FieldState *state;
+	uint32_t n_fields;
+	uint32_t *notok;  // 3 * n_fields, zeroed before the launch
+	uint32_t *bar;    // [0] arrivals (zeroed), [1] abort, [2] error bits
+	unsigned long long *steps;  // null, or 2 words per step: start time (ns), tiles << 32 | live fields
+	uint32_t steps_cap;
+};
 
-// Tile plan of the next step, in the serial section (one CTA).
-__device__ void ptp_plan(const PtpArgs &a)
+__device__ __forceinline__ unsigned long long global_ns()
 {
-	PlanDev *plan = a.plan;
-	__shared__ uint32_t carry_f, carry_t;
-	if(threadIdx.x == 0) { carry_f = 0; carry_t = 0; }
+	unsigned long long t;
+	asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+	return t;
+}
+
+struct SchedSmem {
+	uint32_t i, j, d, iter, n_iter, max_iter, nl, live, win_s, win_e, chk_e, grid;
+};
+
+// Counting barrier: arrival is a release-add, the wait an acquire spin until
+// every CTA of the step has arrived.  Bounded: gives up after SPIN_LIMIT polls
+// (error bit set, abort raised, caller returns).
+__device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t target)
+{
+	__shared__ uint32_t s_ok;
 	__syncthreads();
-	for(uint32_t base = 0; base < a.n_fields; base += NT)
-	{
-		const uint32_t f = base + threadIdx.x;
-		uint32_t tiles = 0;
-		if(f < a.n_fields && ldcg(&a.state[f].live))
-			tiles = (ldcg(&a.state[f].win_e) - ldcg(&a.state[f].win_s) + NT - 1) / NT;
-		const uint32_t is_act = tiles > 0;
-		uint32_t tot_a, tot_t;
-		const uint32_t ia = block_exclusive_scan<NT>(is_act, &tot_a);
-		const uint32_t it = block_exclusive_scan<NT>(tiles, &tot_t);
-		if(is_act)
-		{
-			plan->act[carry_f + ia] = f;
-			plan->tile_start[carry_f + ia] = carry_t + it;
-		}
-		__syncthreads();
-		if(threadIdx.x == 0) { carry_f += tot_a; carry_t += tot_t; }
-		__syncthreads();
-	}
 	if(threadIdx.x == 0)
 	{
-		plan->n_act = carry_f;
-		plan->total_tiles = carry_t;
-		plan->tile_start[carry_f] = carry_t;
-		plan->live = carry_f > 0;
-		plan->step++;
+		s_ok = 1;
+		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+		uint32_t spins = 0;
+		while(ld_acquire(bar) < target)
+		{
+			if(++spins > SPIN_LIMIT || ld_relaxed(bar + 1))
+			{
+				atomicOr(bar + 2, DEV_ERR_TIMEOUT);
+				atomicExch(bar + 1, 1u);
+				s_ok = 0;
+				break;
+			}
+		}
 	}
 	__syncthreads();
+	return s_ok != 0;
 }
 
-// First serial section: open the first sweep of every big field.
-__device__ void ptp_start(const PtpArgs &a)
+// Tiles of every live window (TV window vertices per tile); ts[G] = total.
+template <uint32_t TV>
+__device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uint32_t G)
 {
-	for(uint32_t f = threadIdx.x; f < a.n_fields; f += NT)
-	{
-		FieldState &st = a.state[f];
-		if(!st.big) continue;
-		open_sweep(a.fields[f], st);
-	}
-	if(threadIdx.x == 0) a.plan->step = 0;
+	__shared__ uint32_t carry;
+	if(threadIdx.x == 0) carry = 0;
 	__syncthreads();
-	ptp_plan(a);
-}
-
-// Serial section after a sweep: the reference's schedule update
-// (src/cuda/geodesics_ptp.cu:224-228), then the next sweep's window.
-__device__ void ptp_advance(const PtpArgs &a)
-{
-	const uint32_t n_act = ldcg(&a.plan->n_act);
-	for(uint32_t ai = threadIdx.x; ai < n_act; ai += NT)
+	for(uint32_t base = 0; base < G; base += NT)
 	{
-		const uint32_t f = ldcg(a.plan->act + ai);
-		const FieldDev &F = a.fields[f];
-		FieldState *g = a.state + f;
-		// private copy: every field is owned by one thread of the serial CTA
-		FieldState st = {};
-		st.i = ldcg(&g->i);
-		st.j = ldcg(&g->j);
-		st.d = ldcg(&g->d);
-		st.iter = ldcg(&g->iter);
-		st.max_iter = ldcg(&g->max_iter);
-		st.n_iter = ldcg(&g->n_iter);
-		st.win_s = ldcg(&g->win_s);
-		st.win_e = ldcg(&g->win_e);
-		st.relax = ldcg(&g->relax);
-		const uint32_t nl = ldcg(&g->n_limits);
-		st.relax += st.win_e - st.win_s;
-		if(!ldcg(&g->notok)) st.i++;
-		if(st.j < nl - 1) st.j++;
-		st.d ^= 1u;
-		st.n_iter++;
-		open_sweep(F, st);
-		g->i = st.i;
-		g->j = st.j;
-		g->d = st.d;
-		g->iter = st.iter;
-		g->n_iter = st.n_iter;
-		g->relax = st.relax;
-		g->notok = 0;
-		g->live = st.live;
-		g->win_s = st.win_s;
-		g->win_e = st.win_e;
-		g->chk_e = st.chk_e;
+		const uint32_t q = base + threadIdx.x;
+		const uint32_t tiles = q < G && fs[q].live ? (fs[q].win_e - fs[q].win_s + TV - 1) / TV : 0u;
+		uint32_t tot;
+		const uint32_t ex = block_exclusive_scan<NT>(tiles, &tot);
+		if(q < G) ts[q] = carry + ex;
+		__syncthreads();
+		if(threadIdx.x == 0) carry += tot;
+		__syncthreads();
 	}
+	if(threadIdx.x == 0) ts[G] = carry;
 	__syncthreads();
-	ptp_plan(a);
 }
 
 template <typename T, bool CL>
-__global__ void __launch_bounds__(NT) ptp_kernel(PtpArgs a)
+__global__ void __launch_bounds__(NT, 3) ptp_kernel(GridArgs a)
 {
-	uint32_t gen = 0;
-	if(!grid_sync(a.sync, gen, [&] { ptp_start(a); })) return;
+	extern __shared__ __align__(16) unsigned char smem[];
+	const uint32_t F = a.n_fields;
+	// compacted: entry q describes field id[q]; only fields handed to the grid.
+	// Layout: 8-byte counters first, then 4-byte-aligned arrays.
+	unsigned long long *rx = reinterpret_cast<unsigned long long *>(smem);
+	SchedSmem *fs = reinterpret_cast<SchedSmem *>(rx + F);
+	uint32_t *ts = reinterpret_cast<uint32_t *>(fs + F);
+	uint32_t *id = ts + F + 1;
+	__shared__ uint32_t s_G;
 	const uint32_t lane = threadIdx.x & 31;
+	constexpr uint32_t TV = NT;  // window vertices per tile
 
-	for(;;)
+	if(threadIdx.x == 0) s_G = 0;
+	__syncthreads();
+	for(uint32_t base = 0; base < F; base += NT)
 	{
-		if(!ld_relaxed(&a.plan->live) || ld_relaxed(&a.sync->abort)) break;
-		const uint32_t T_tiles = ldcg(&a.plan->total_tiles);
-		const uint32_t n_act = ldcg(&a.plan->n_act);
-		for(uint32_t k = blockIdx.x; k < T_tiles; k += gridDim.x)
+		const uint32_t f = base + threadIdx.x;
+		const bool on = f < F && a.state[f].big && a.state[f].live;
+		uint32_t tot;
+		const uint32_t ex = block_exclusive_scan<NT>(on ? 1u : 0u, &tot);
+		if(on)
 		{
-			const uint32_t ai = upper_index<true>(a.plan->tile_start, n_act, k);
-			const uint32_t f = ldcg(a.plan->act + ai);
-			const FieldDev &F = a.fields[f];
-			const FieldState *stp = a.state + f;
-			const uint32_t d = ldcg(&stp->d);
-			const uint32_t win_e = ldcg(&stp->win_e), chk_e = ldcg(&stp->chk_e);
-			const uint32_t v = ldcg(&stp->win_s) + (k - ldcg(a.plan->tile_start + ai)) * NT + threadIdx.x;
-			int bad = 0;
-			if(v < win_e) bad = sweep_vertex<T, CL, true>(F, d, v, chk_e);
-			// one atomic per warp that saw a failure, no block barrier per tile
-			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.state[f].notok, 1u);
+			const FieldState &g = a.state[f];
+			const uint32_t q = s_G + ex;
+			SchedSmem &x = fs[q];
+			id[q] = f;
+			x.grid = 1;
+			x.live = 1;
+			x.i = g.i;
+			x.j = g.j;
+			x.d = g.d;
+			x.iter = g.iter;
+			x.n_iter = g.n_iter;
+			x.max_iter = g.max_iter;
+			x.nl = g.n_limits;
+			x.win_s = g.win_s;
+			x.win_e = g.win_e;
+			x.chk_e = g.chk_e;
+			rx[q] = g.relax;
 		}
-		if(!grid_sync(a.sync, gen, [&] { ptp_advance(a); })) return;
+		__syncthreads();
+		if(threadIdx.x == 0) s_G += tot;
+		__syncthreads();
 	}
+	const uint32_t G = s_G;
+	grid_plan<TV>(fs, ts, G);
+
+	for(uint32_t step = 0;; step++)
+	{
+		const uint32_t total = ts[G];
+		if(blockIdx.x == 0 && threadIdx.x == 0 && a.steps && step < a.steps_cap)
+		{
+			uint32_t live = 0;
+			for(uint32_t q = 0; q < G; q++) live += fs[q].live;
+			a.steps[2 * step] = global_ns();
+			a.steps[2 * step + 1] = ((unsigned long long) total << 32) | live;
+		}
+		if(!total) break;
+		uint32_t *flags = a.notok + (step % 3) * F;
+		for(uint32_t k = blockIdx.x; k < total; k += gridDim.x)
+		{
+			uint32_t lo = 0, hi = G;  // last entry whose first tile <= k
+			while(hi - lo > 1)
+			{
+				const uint32_t mid = (lo + hi) >> 1;
+				if(ts[mid] <= k) lo = mid;
+				else hi = mid;
+			}
+			const SchedSmem &x = fs[lo];
+			const uint32_t f = id[lo];
+			int bad = 0;
+			const uint32_t v = x.win_s + (k - ts[lo]) * TV + threadIdx.x;
+			if(v < x.win_e) bad = sweep_vertex<T, CL, true>(a.fields[f], x.d, v, x.chk_e);
+			// one atomic per warp that saw a failure, no block barrier per tile
+			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
+		}
+		if(!count_barrier(a.bar, gridDim.x * (step + 1))) return;
+		// every CTA advances its own copy of every schedule
+		for(uint32_t q = threadIdx.x; q < G; q += NT)
+		{
+			SchedSmem &x = fs[q];
+			const uint32_t f = id[q];
+			if(blockIdx.x == 0) a.notok[((step + 2) % 3) * F + f] = 0;
+			if(!x.live) continue;
+			FieldState st = {};
+			st.i = x.i;
+			st.j = x.j;
+			st.d = x.d;
+			st.iter = x.iter;
+			st.n_iter = x.n_iter;
+			st.max_iter = x.max_iter;
+			st.n_limits = x.nl;
+			st.win_s = x.win_s;
+			st.win_e = x.win_e;
+			st.relax = rx[q];
+			close_sweep(st, !ldcg(flags + f));
+			open_sweep(a.fields[f], st, blockIdx.x == 0);
+			x.i = st.i;
+			x.j = st.j;
+			x.d = st.d;
+			x.iter = st.iter;
+			x.n_iter = st.n_iter;
+			x.live = st.live;
+			x.win_s = st.win_s;
+			x.win_e = st.win_e;
+			x.chk_e = st.chk_e;
+			rx[q] = st.relax;
+		}
+		__syncthreads();
+		grid_plan<TV>(fs, ts, G);
+	}
+	if(blockIdx.x == 0)
+		for(uint32_t q = threadIdx.x; q < G; q += NT)
+		{
+			const SchedSmem &x = fs[q];
+			FieldState &g = a.state[id[q]];
+			g.i = x.i;
+			g.j = x.j;
+			g.d = x.d;
+			g.iter = x.iter;
+			g.n_iter = x.n_iter;
+			g.live = 0;
+			g.relax = rx[q];
+		}
+}
+
+size_t grid_smem_bytes(uint32_t F)
+{
+	static_assert(sizeof(SchedSmem) % 4 == 0, "layout");
+	return 8 * (size_t) F + sizeof(SchedSmem) * F + 4 * (size_t) (F + 1) + 4 * (size_t) F;
 }
 
 // ---------------------------------------------------------------------------
@@ -585,8 +780,10 @@ __global__ void fill_kernel(CatArgs c)
 		const FieldState &st = c.state[f];
 		const uint32_t nr = st.n_limits ? F.limits[st.n_limits - 1] : 0;
 		const uint32_t n0 = st.n_limits >= 2 ? F.limits[1] : nr;
-		T *D0 = static_cast<T *>(F.D[0]);
-		T *D1 = static_cast<T *>(F.D[1]);
+		// FP32 path: double-float (hi, lo) pairs; FP64 path: double
+		using S = typename std::conditional<sizeof(T) == 4, float2, double>::type;
+		S *D0 = static_cast<S *>(F.D[0]);
+		S *D1 = static_cast<S *>(F.D[1]);
 		if(k < nr)
 		{
 			const uint32_t v = F.sorted[k];
@@ -603,12 +800,15 @@ __global__ void fill_kernel(CatArgs c)
 			F.P[k] = F.m.pos[v];
 			if(F.Pd)
 			{
-				F.Pd[4 * (size_t) k] = F.m.posd[4 * (size_t) v];
-				F.Pd[4 * (size_t) k + 1] = F.m.posd[4 * (size_t) v + 1];
-				F.Pd[4 * (size_t) k + 2] = F.m.posd[4 * (size_t) v + 2];
+				const float4 pf = F.m.pos[v];
+				F.Pd[4 * (size_t) k] = F.round_coords ? (double) pf.x : F.m.posd[4 * (size_t) v];
+				F.Pd[4 * (size_t) k + 1] = F.round_coords ? (double) pf.y : F.m.posd[4 * (size_t) v + 1];
+				F.Pd[4 * (size_t) k + 2] = F.round_coords ? (double) pf.z : F.m.posd[4 * (size_t) v + 2];
 				F.Pd[4 * (size_t) k + 3] = 0.0;
 			}
-			const T d0 = k < n0 ? T(0) : T(INFINITY);
+			S d0;
+			if constexpr(sizeof(T) == 4) d0 = make_float2(k < n0 ? 0.f : INFINITY, 0.f);
+			else d0 = k < n0 ? 0.0 : (double) INFINITY;
 			D0[k] = d0;
 			D1[k] = d0;
 			if(CL)
@@ -627,8 +827,16 @@ __global__ void fill_kernel(CatArgs c)
 			F.P[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 			if(F.Pd)
 				for(int q = 0; q < 4; q++) F.Pd[4 * (size_t) k + q] = 0.0;
-			D0[k] = T(INFINITY);
-			D1[k] = T(INFINITY);
+			if constexpr(sizeof(T) == 4)
+			{
+				D0[k] = make_float2(INFINITY, 0.f);
+				D1[k] = make_float2(INFINITY, 0.f);
+			}
+			else
+			{
+				D0[k] = (double) INFINITY;
+				D1[k] = (double) INFINITY;
+			}
 			if(CL) { F.C[0][k] = 0; F.C[1][k] = 0; }
 		}
 	}
@@ -646,8 +854,14 @@ __global__ void gather_kernel(CatArgs c)
 		const FieldState &st = c.state[f];
 		const uint32_t iv = F.inv[v];
 		const uint32_t k = iv ? iv - 1 : st.nr;
-		const T x = static_cast<const T *>(F.D[st.d])[k];
-		if(F.out_f64) static_cast<double *>(F.dist_out)[v] = (double) x;
+		double x;
+		if constexpr(sizeof(T) == 4)
+		{
+			const float2 h = static_cast<const float2 *>(F.D[st.d])[k];
+			x = (double) h.x + (double) h.y;
+		}
+		else x = static_cast<const double *>(F.D[st.d])[k];
+		if(F.out_f64) static_cast<double *>(F.dist_out)[v] = x;
 		else static_cast<float *>(F.dist_out)[v] = (float) x;
 		if(CL && F.clusters_out)
 			F.clusters_out[v] = iv ? F.C[st.d][k] : (F.clusters_in ? F.clusters_in[v] : 0u);
@@ -758,15 +972,40 @@ static const void *ptp_kernel_ptr(bool f64, bool clusters)
 	return clusters ? (const void *) ptp_kernel<float, true> : (const void *) ptp_kernel<float, false>;
 }
 
-int ptp_max_ctas(int device, bool f64, bool clusters)
+// grid launches keep the schedules of up to this many fields in shared memory
+constexpr uint32_t GRID_MAX_FIELDS = 2048;
+
+// CTAs of a grid launch over n_fields fields: every SM's share at the shared
+// memory this launch really uses (the schedule copy grows with n_fields).
+int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields)
 {
 	int nsm = 0, per = 0;
 	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
-	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ptp_kernel_ptr(f64, clusters), NT, 0);
+	const void *k = ptp_kernel_ptr(f64, clusters);
+	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) grid_smem_bytes(GRID_MAX_FIELDS));
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NT, grid_smem_bytes(std::max<uint32_t>(n_fields, 1)));
 	return nsm * per;
 }
 
 int ptp_threads() { return NT; }
+
+uint32_t ptp_grid_max_fields() { return GRID_MAX_FIELDS; }
+
+// notok: 3 * n_fields words; bar: 4 words.  Both zeroed here.
+cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
+                       uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
+                       cudaStream_t s)
+{
+	if(!n_fields) return cudaSuccess;
+	cudaError_t e = cudaMemsetAsync(notok, 0, 3 * sizeof(uint32_t) * n_fields, s);
+	if(e == cudaSuccess) e = cudaMemsetAsync(bar, 0, 4 * sizeof(uint32_t), s);
+	if(e == cudaSuccess && steps) e = cudaMemsetAsync(steps, 0, 16 * (size_t) steps_cap, s);
+	if(e != cudaSuccess) return e;
+	GridArgs a{fields, state, n_fields, notok, bar, steps, steps_cap};
+	void *args[] = {&a};
+	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters), dim3(ctas), dim3(NT), args,
+	                                   grid_smem_bytes(n_fields), s);
+}
 
 static const void *ptp_local_ptr(bool f64, bool clusters)
 {
@@ -793,23 +1032,13 @@ cudaError_t launch_classify(FieldDev *fields, FieldState *state, uint32_t n_fiel
 
 // queue: one word, zeroed here (the field ticket)
 cudaError_t launch_ptp_local(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
-                             uint32_t ctas, bool f64, bool clusters, cudaStream_t s)
+                             uint32_t ctas, uint32_t local_window, bool f64, bool clusters, cudaStream_t s)
 {
 	cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
 	if(e != cudaSuccess) return e;
 	ctas = std::max<uint32_t>(1, std::min<uint32_t>(ctas, n_fields));
-	void *args[] = {&fields, &state, &n_fields, &queue};
+	void *args[] = {&fields, &state, &n_fields, &queue, &local_window};
 	return cudaLaunchKernel(ptp_local_ptr(f64, clusters), dim3(ctas), dim3(LT), args, 0, s);
-}
-
-cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, PlanDev *plan, GridSync *sync,
-                       uint32_t ctas, bool f64, bool clusters, cudaStream_t s)
-{
-	PtpArgs a{fields, state, n_fields, plan, sync};
-	void *args[] = {&a};
-	cudaError_t e = cudaMemsetAsync(sync, 0, sizeof(GridSync), s);
-	if(e != cudaSuccess) return e;
-	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters), dim3(ctas), dim3(NT), args, 0, s);
 }
 
 cudaError_t launch_normalize(void *dist, bool f64, uint64_t n, unsigned long long *tmp, cudaStream_t s)

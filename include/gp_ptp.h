@@ -112,7 +112,9 @@ typedef struct gp_ptp_opts {
 	uint32_t ctas;         /* CTAs of the grid-wide launch, 0: all that fit */
 	uint32_t local_window; /* fields whose windows stay within this many vertices are
 	                          swept by one CTA each; 0: default (4096) */
-	uint32_t reserved[3];
+	uint32_t round_coords; /* GP_F64 only: 1 = solve on the float-rounded coordinates
+	                          the GP_F32 path sees (an FP64 check of an FP32 run) */
+	uint32_t reserved[2];
 } gp_ptp_opts;
 
 typedef struct gp_ptp_stats {
@@ -164,6 +166,37 @@ typedef struct gp_field {
 gp_status gp_ptp_batch(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields,
                        const gp_ptp_opts *opts, gp_dtype dist_type, uint32_t flags,
                        double *seconds);
+
+/* Device timings and counts of the last gp_ptp / gp_ptp_batch / gp_toplesets
+ * call on a context (CUDA events between the phases, on the context's stream).
+ * No reference counterpart: the reference times a whole call with one event
+ * pair (src/cuda/geodesics_ptp.cu:24-84). */
+typedef struct gp_call_stats {
+	uint32_t launches;         /* kernels this library launched in the call */
+	uint32_t n_fields;
+	uint32_t fields_grid;      /* fields swept by the grid-wide launch */
+	uint32_t sweeps_grid;      /* steps of the grid-wide launch */
+	double ms_toplesets;       /* BFS setup + BFS */
+	double ms_renumber;        /* ring renumbering passes */
+	double ms_local;           /* classify + one-CTA-per-field sweeps */
+	double ms_grid;            /* grid-wide persistent sweeps */
+	double ms_gather;          /* output gather */
+	uint64_t relax_local;      /* vertex relaxations done by the one-CTA launch */
+	uint64_t relax_grid;       /* vertex relaxations done by the grid-wide launch */
+	uint64_t h2d_bytes;        /* host -> device bytes copied by the call */
+	uint64_t d2h_bytes;        /* device -> host bytes copied by the call */
+} gp_call_stats;
+
+gp_status gp_ctx_call_stats(const gp_ctx *ctx, gp_call_stats *out);
+
+/* Step trace of the grid-wide sweep launch.  With out == null: arm the trace
+ * for up to cap steps of the following calls (cap = 0 disarms).  Otherwise
+ * copy the last call's trace: 2 words per step, the step's start time (ns,
+ * device global timer) and (tiles << 32 | live fields); *n_out = steps.
+ * Used to study and learn the sweep schedule.  No reference counterpart (the
+ * reference writes a per-iteration "band" file in its test harness,
+ * src/cuda/test_geodesics_ptp_coalescence.cu:214-266). */
+gp_status gp_ctx_step_trace(gp_ctx *ctx, uint32_t cap, uint64_t *out, uint32_t *n_out);
 
 /* normalize_ptp (src/geodesics_ptp.cpp:264-276) on a host array. */
 gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n);

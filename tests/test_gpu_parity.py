@@ -123,19 +123,24 @@ def test_clusters_gpu_rule(gpu_ctx, oracle_lib):
     assert set(np.unique(cl)) == {1, 2, 3}
 
 
-def test_batch_equals_single_fields(gpu_ctx):
+@pytest.mark.parametrize("n_fields", [12, 13, 40])
+def test_batch_equals_single_fields(gpu_ctx, n_fields):
+    """Batched fields (some swept by one CTA, some handed to the grid-wide
+    launch: the 200^2 height field's windows outgrow one CTA) equal the same
+    fields solved alone, bit for bit; odd and even batch sizes."""
     from gproshan_gb300 import _capi, meshgen
     meshes = [dev_mesh(gpu_ctx, *meshgen.icosphere(3, 0.1, 1)), dev_mesh(gpu_ctx, *meshgen.height_field(70, 2)),
-              dev_mesh(gpu_ctx, *meshgen.icosphere(5, 0.1, 3)), dev_mesh(gpu_ctx, *meshgen.height_field(33, 8))]
-    rng = np.random.default_rng(0)
+              dev_mesh(gpu_ctx, *meshgen.icosphere(5, 0.1, 3)), dev_mesh(gpu_ctx, *meshgen.height_field(200, 8))]
+    rng = np.random.default_rng(n_fields)
     ms, srcs = [], []
-    for k in range(12):
+    for k in range(n_fields):
         mm = meshes[k % len(meshes)]
         ms.append(mm)
         srcs.append(rng.choice(mm.n_vertices, size=1 + k % 3, replace=False))
     dists, stats, sec = _capi.ptp_batch(gpu_ctx, ms, srcs)
     assert sec > 0
-    for k in range(12):
+    assert gpu_ctx.call_stats().fields_grid >= 1  # the grid-wide launch did run
+    for k in range(n_fields):
         d, _, st = _capi.ptp(ms[k], srcs[k])
         assert np.array_equal(d, dists[k]), k
         assert st.n_iter == stats[k].n_iter
