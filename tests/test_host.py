@@ -94,3 +94,19 @@ def test_unsupported_options_raise(built_lib):
     xyz, tri = meshgen.icosphere(1, 0.0, 0)
     with pytest.raises(NotImplementedError):
         geodesics(che(xyz, tri), [0], geodesics.FM)
+
+
+def test_cpp_dropin_shim_compiles_against_reference_headers():
+    """The C++ shim that replaces src/cuda/geodesics_ptp*.cu compiles against
+    the reference's own headers (FP64 and SINGLE_P builds)."""
+    import shutil
+    import subprocess
+    ref = "/root/reference/include"
+    if not os.path.isdir(ref) or not shutil.which("g++"):
+        pytest.skip("reference checkout or g++ not present")
+    shim = os.path.join(ROOT, "gproshan_gb300", "shim", "geodesics_ptp_gb300.cpp")
+    for extra in ([], ["-DSINGLE_P"]):
+        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-fopenmp", *extra,
+                            "-I", os.path.join(ROOT, "oracle", "stubs"), "-I", ref,
+                            "-I", os.path.join(ROOT, "include"), shim], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
