@@ -91,6 +91,8 @@ SIGNATURES = {
     "gp_normalize_ptp": (C.c_int, [C.c_void_p, C.c_void_p, C.c_int, C.c_uint64]),
     "gp_ctx_call_stats": (C.c_int, [C.c_void_p, C.POINTER(gp_call_stats)]),
     "gp_ctx_step_trace": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32)]),
+    "gp_toplesets_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
+                                       C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
     "gp_fps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64,
                          C.c_double, C.POINTER(gp_ptp_opts), _u32p, C.POINTER(C.c_double),
                          C.POINTER(C.c_double)]),

@@ -547,6 +547,11 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 
 } // namespace
 
+namespace gp {
+const MeshDev *mesh_dev(const gp_mesh *mesh) { return mesh ? &mesh->dev : nullptr; }
+int mesh_device(const gp_mesh *mesh) { return mesh && mesh->ctx ? mesh->ctx->device : -1; }
+} // namespace gp
+
 // ===========================================================================
 // C ABI
 // ===========================================================================

@@ -128,4 +128,8 @@ int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields);
 cudaError_t launch_argmax_abs(const void *dist, bool f64, uint32_t n, unsigned long long *out,
                               cudaStream_t s);
 
+// gp_capi.cpp: a mesh's device arrays and the device that holds them
+const MeshDev *mesh_dev(const gp_mesh *mesh);
+int mesh_device(const gp_mesh *mesh);
+
 } // namespace gp

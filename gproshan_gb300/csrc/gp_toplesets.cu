@@ -15,6 +15,8 @@
 //   emit:     frontier chunks in `sorted` order; each vertex counts the u
 //             whose key it holds, a block scan (carried across chunks) gives
 //             their positions, and the owners write them and set ring[u].
+#include <mutex>
+
 #include "gp_common.cuh"
 
 namespace gp {
@@ -176,4 +178,125 @@ cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fie
 	return cudaGetLastError();
 }
 
+// ---------------------------------------------------------------------------
+// Toplesets without any device allocation (gp_toplesets_noalloc).
+//
+// Some callers may not allocate device memory while they compute: an
+// application that has handed all device memory to its own pool up front, or
+// a latency-critical loop in which cudaMalloc/cudaFree (which can stall the
+// whole device) are not allowed.  For them the BFS scratch -- the per-vertex
+// discovery keys and the small field descriptor -- lives in one fixed
+// file-scope device array instead of the context workspace.  Every GPU that
+// loads this library reserves that array until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr uint32_t NOALLOC_MAX_VERTICES = 1u << 20;  // largest mesh the array serves
+constexpr size_t NOALLOC_HEADER = 4096;               // field descriptor, state, queue
+
+struct NoallocHeader {
+	FieldDev f;
+	FieldState st;
+	uint32_t vbase[2];
+	uint32_t queue;
+};
+static_assert(sizeof(NoallocHeader) <= NOALLOC_HEADER, "header size");
+
+// header, then 8-byte keys for up to NOALLOC_MAX_VERTICES vertices (about 8 MiB)
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_HEADER + 8ull * NOALLOC_MAX_VERTICES];
+
+// Writes this call's descriptor into the array and clears what must start at
+// zero (the queue ticket and the field state); the keys are reset by
+// bfs_clear_kernel.  Earlier calls' contents are otherwise left in place.
+__global__ void noalloc_setup_kernel(MeshDev m, const uint32_t *src, uint32_t ns, uint32_t *rings, uint32_t *sorted,
+                                     uint32_t cap_sorted, uint32_t *limits)
+{
+	if(threadIdx.x != 0) return;
+	NoallocHeader *h = reinterpret_cast<NoallocHeader *>(g_noalloc_scratch);
+	FieldDev f;
+	memset(&f, 0, sizeof(f));
+	f.m = m;
+	f.src = src;
+	f.ns = ns;
+	f.cap_sorted = cap_sorted;
+	f.ring = rings;
+	f.key = reinterpret_cast<unsigned long long *>(g_noalloc_scratch + NOALLOC_HEADER);
+	f.sorted = sorted;
+	f.limits = limits;
+	h->f = f;
+	memset(&h->st, 0, sizeof(h->st));
+	h->vbase[0] = 0;
+	h->vbase[1] = m.nv;
+	h->queue = 0;
+}
+
+__global__ void noalloc_finish_kernel(uint32_t *n_limits)
+{
+	if(threadIdx.x != 0) return;
+	const NoallocHeader *h = reinterpret_cast<const NoallocHeader *>(g_noalloc_scratch);
+	*n_limits = h->st.status ? 0u : h->st.n_limits;
+}
+
+std::mutex g_noalloc_mu;
+void *g_noalloc_ptr[64] = {};
+
+// Device address of the array on the current device, looked up once per
+// device (the symbol's host-side name is not a device address).
+gp_status noalloc_scratch(void **out)
+{
+	int dev = -1;
+	if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
+	{
+		cudaGetLastError();
+		return GP_ERR_NO_DEVICE;
+	}
+	std::lock_guard<std::mutex> lock(g_noalloc_mu);
+	if(!g_noalloc_ptr[dev])
+	{
+		void *p = nullptr;
+		const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		if(e != cudaSuccess || !p)
+		{
+			cudaGetLastError();
+			return GP_ERR_CUDA;
+		}
+		g_noalloc_ptr[dev] = p;
+	}
+	*out = g_noalloc_ptr[dev];
+	return GP_OK;
+}
+
+} // namespace
+
 } // namespace gp
+
+extern "C" gp_status gp_toplesets_noalloc(const gp_mesh *mesh, const uint32_t *sources, uint32_t n_sources,
+                                          uint32_t *rings, uint32_t *sorted, uint32_t cap_sorted, uint32_t *limits,
+                                          uint32_t cap_limits, uint32_t *n_limits, void *stream)
+{
+	using namespace gp;
+	if(!mesh || !sources || !n_sources || !rings || !sorted || !limits || !n_limits) return GP_ERR_INVALID_ARG;
+	const MeshDev *m = mesh_dev(mesh);
+	if(m->nv > NOALLOC_MAX_VERTICES) return GP_ERR_CAPACITY;  // the fixed array holds 2^20 vertices
+	if((uint64_t) cap_sorted < (uint64_t) m->nv + n_sources || (uint64_t) cap_limits < (uint64_t) m->nv + 2)
+		return GP_ERR_CAPACITY;
+	int dev = -1;
+	if(cudaGetDevice(&dev) != cudaSuccess || dev != mesh_device(mesh))
+	{
+		cudaGetLastError();
+		return GP_ERR_INVALID_ARG;  // the mesh's device must be current
+	}
+	void *base = nullptr;
+	const gp_status st = noalloc_scratch(&base);
+	if(st != GP_OK) return st;
+	NoallocHeader *h = static_cast<NoallocHeader *>(base);
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
+	noalloc_setup_kernel<<<1, 32, 0, s>>>(*m, sources, n_sources, rings, sorted, cap_sorted, limits);
+	bfs_clear_kernel<<<(unsigned) std::min<uint32_t>((m->nv + 255) / 256, 152 * 16), 256, 0, s>>>(&h->f, h->vbase, 1,
+	                                                                                              m->nv);
+	bfs_seed_kernel<<<1, 32, 0, s>>>(&h->f, &h->st, 1);
+	bfs_kernel<<<1, BT, 0, s>>>(&h->f, &h->st, 1, &h->queue);
+	noalloc_finish_kernel<<<1, 32, 0, s>>>(n_limits);
+	return cudaGetLastError() == cudaSuccess ? GP_OK : GP_ERR_CUDA;
+}
+

@@ -198,6 +198,33 @@ gp_status gp_ctx_call_stats(const gp_ctx *ctx, gp_call_stats *out);
  * src/cuda/test_geodesics_ptp_coalescence.cu:214-266). */
 gp_status gp_ctx_step_trace(gp_ctx *ctx, uint32_t cap, uint64_t *out, uint32_t *n_out);
 
+/*
+ * gp_toplesets without any device allocation, for callers that may not
+ * allocate device memory while they work (an application that gave all device
+ * memory to its own pool up front, a latency-critical loop where cudaMalloc /
+ * cudaFree, which can stall the device, are not allowed).  No reference
+ * counterpart: it is che::compute_toplesets' result (src/che.cpp:546-593)
+ * computed into caller-provided DEVICE buffers.
+ *
+ * The BFS scratch (8 bytes per vertex plus a 4 KiB descriptor) is a fixed
+ * array inside the library, about 8 MiB, reserved on every GPU that loads the
+ * library until the process exits; meshes above 2^20 vertices get
+ * GP_ERR_CAPACITY.  The mesh's device must be current.  The first call on a
+ * device looks up the array's device address (cudaGetSymbolAddress); make that
+ * first call before any stream capture.  Work is enqueued on `stream` (a
+ * cudaStream_t, 0 = default stream) and the call returns without waiting.
+ * All calls share the one array: calls that overlap on the GPU (other streams,
+ * other threads) race and must be serialised by the caller.
+ *
+ * sources: device array of n_sources vertex ids.  rings[n_vertices],
+ * sorted[cap_sorted >= n_vertices + n_sources], limits[cap_limits >=
+ * n_vertices + 2]: device outputs as gp_toplesets writes them.  *n_limits
+ * (device word) receives |limits|, or 0 if a source is out of range.
+ */
+gp_status gp_toplesets_noalloc(const gp_mesh *mesh, const uint32_t *sources, uint32_t n_sources,
+                               uint32_t *rings, uint32_t *sorted, uint32_t cap_sorted, uint32_t *limits,
+                               uint32_t cap_limits, uint32_t *n_limits, void *stream);
+
 /* normalize_ptp (src/geodesics_ptp.cpp:264-276) on a host array. */
 gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n);
 
