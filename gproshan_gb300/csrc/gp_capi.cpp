@@ -16,6 +16,7 @@ namespace gp {
 cudaError_t launch_fan_fill(const uint32_t *VT, const uint32_t *OT, const uint32_t *EVT, uint32_t nv,
                             const uint32_t *flags, uint32_t *off, uint32_t *fan, cudaStream_t s);
 cudaError_t launch_strip_flags(const uint32_t *in, uint32_t *out, uint32_t n, cudaStream_t s);
+cudaError_t launch_fan8(const uint32_t *off, const uint32_t *fan, uint32_t nv, uint4 *rows, cudaStream_t s);
 cudaError_t launch_bfs_setup(FieldDev *fields, FieldState *state, const uint32_t *vbase, uint32_t n_fields,
                              uint32_t total_vertices, cudaStream_t s);
 cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
@@ -283,6 +284,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
 	const size_t o_sorted = cv.add<uint32_t>(tot), o_lim = cv.add<uint32_t>(tot), o_inv = cv.add<uint32_t>(tot);
 	size_t o_cnt = 0, o_scan = 0, o_P = 0, o_Pd = 0, o_off = 0, o_fan = 0, o_D0 = 0, o_D1 = 0, o_C0 = 0, o_C1 = 0;
+	size_t o_fan8 = 0;
 	size_t o_out = 0, o_cout = 0, o_cin = 0;
 	if(stage == Stage::ptp)
 	{
@@ -291,6 +293,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		o_P = cv.add<float4>(tot);
 		if(f64) o_Pd = cv.add<double>(4 * tot);
 		o_off = cv.add<uint32_t>(tot);
+		o_fan8 = cv.add<uint4>(2 * tot);
 		o_fan = cv.add<uint32_t>(ftot);
 		o_D0 = cv.add<char>(tot * tsz);
 		o_D1 = cv.add<char>(tot * tsz);
@@ -332,6 +335,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			d.P = reinterpret_cast<float4 *>(P(o_P)) + base[f];
 			d.Pd = f64 ? reinterpret_cast<double *>(P(o_Pd)) + 4ull * base[f] : nullptr;
 			d.off = reinterpret_cast<uint32_t *>(P(o_off)) + base[f];
+			d.fan8 = reinterpret_cast<uint4 *>(P(o_fan8)) + 2ull * base[f];
 			d.fan = reinterpret_cast<uint32_t *>(P(o_fan));
 			d.D[0] = P(o_D0) + (size_t) base[f] * tsz;
 			d.D[1] = P(o_D1) + (size_t) base[f] * tsz;
@@ -803,6 +807,7 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 	Carve mc;
 	const size_t m_pos = mc.add<float4>(nv), m_posd = mc.add<double>(4 * (size_t) nv);
 	const size_t m_off = mc.add<uint32_t>(nv + 1), m_fan = mc.add<uint32_t>(n_fan);
+	const size_t m_fan8 = mc.add<uint4>(2 * (size_t) nv);
 	cudaError_t e = cudaMalloc(&m->block, mc.off);
 	if(e != cudaSuccess)
 	{
@@ -815,12 +820,14 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 	m->dev.posd = reinterpret_cast<double *>(B + m_posd);
 	m->dev.fan_off = reinterpret_cast<uint32_t *>(B + m_off);
 	m->dev.fan = reinterpret_cast<uint32_t *>(B + m_fan);
+	m->dev.fan8 = reinterpret_cast<uint4 *>(B + m_fan8);
 	m->dev.nv = nv;
 	m->dev.n_fan = n_fan;
 	m->dev.max_fan = h[1];
 	uint32_t *doff = const_cast<uint32_t *>(m->dev.fan_off);
 	e = cudaMemcpyAsync(doff, dcnt, 4 * ((size_t) nv + 1), cudaMemcpyDeviceToDevice, s);
 	if(e == cudaSuccess) e = launch_fan_fill(dvt, dot, devt, nv, dflags, doff, const_cast<uint32_t *>(m->dev.fan), s);
+	if(e == cudaSuccess) e = launch_fan8(doff, m->dev.fan, nv, const_cast<uint4 *>(m->dev.fan8), s);
 	if(e == cudaSuccess)
 		e = launch_pos_convert(reinterpret_cast<double *>(T + t_xyz), nv, const_cast<float4 *>(m->dev.pos),
 		                       const_cast<double *>(m->dev.posd), s);

@@ -13,6 +13,12 @@ constexpr uint32_t NIL = 0xFFFFFFFFu;
 constexpr uint32_t FAN_CLOSED = 0x80000000u;  // bit 31 of fan_off[v]: v's fan is closed
 constexpr uint32_t FAN_MASK = 0x7FFFFFFFu;
 constexpr uint32_t MAX_WALK = 1u << 16;       // longest star walk accepted per vertex
+// Fixed-stride fan rows of the renumbered copy: slots 0..n-1 hold the fan,
+// unused slots FAN8_EMPTY; bit 31 of slot 0 marks a closed fan; a vertex with
+// more than 8 fan entries has slot 7 = FAN8_OVERFLOW and is read from the
+// CSR lists (off/fan) instead.
+constexpr uint32_t FAN8_EMPTY = 0xFFFFFFFFu;
+constexpr uint32_t FAN8_OVERFLOW = 0xFFFFFFFEu;
 
 // trig/next/prev of the compact half-edge mesh (src/che.cpp:18-34)
 __host__ __device__ inline uint32_t he_next(uint32_t he) { return 3 * (he / 3) + (he + 1) % 3; }
@@ -37,6 +43,7 @@ struct MeshDev {
 	const double *posd;      // 4*nv (x, y, z, 0); null unless the FP64 path is enabled
 	const uint32_t *fan_off; // nv+1; entries [fan_off[v]&MASK, fan_off[v+1]&MASK); bit31 = closed
 	const uint32_t *fan;     // link of each vertex in star-walk order (che::link order)
+	const uint4 *fan8;       // 2 * nv: the same links as fixed-stride rows (FAN8_* encoding)
 	uint32_t nv;
 	uint32_t n_fan;
 	uint32_t max_fan;        // largest per-vertex entry count
@@ -60,6 +67,7 @@ struct FieldDev {
 	double *Pd;               // 4*(cap_sorted + 1) or null
 	uint32_t *off;            // cap_sorted + 2 (bit31 = closed)
 	uint32_t *fan;            // renumbered fan entries
+	uint4 *fan8;              // 2 * (cap_sorted + 1): 8 fan slots per vertex (see FAN8_*)
 	void *D[2];               // cap_sorted + 1 distances (float or double)
 	uint32_t *C[2];           // cap_sorted + 1 labels, or null
 	// outputs / inputs in original numbering

@@ -77,6 +77,22 @@ __global__ void fan_fill_kernel(const uint32_t *__restrict__ VT, const uint32_t 
 	off[v] = o | (f & FAN_CLOSED);
 }
 
+// Fixed-stride rows of the links (see FAN8_* in gp_internal.h).
+__global__ void fan8_kernel(const uint32_t *__restrict__ off, const uint32_t *__restrict__ fan, uint32_t nv,
+                            uint4 *__restrict__ rows)
+{
+	const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+	if(v >= nv) return;
+	const uint32_t o0f = off[v], o0 = o0f & FAN_MASK, o1 = off[v + 1] & FAN_MASK;
+	const uint32_t n = o1 - o0;
+	uint32_t r[8];
+	for(uint32_t q = 0; q < 8; q++) r[q] = q < n ? fan[o0 + q] : FAN8_EMPTY;
+	if(n > 8) r[7] = FAN8_OVERFLOW;
+	if(n && (o0f & FAN_CLOSED)) r[0] |= FAN_CLOSED;
+	rows[2 * (size_t) v] = make_uint4(r[0], r[1], r[2], r[3]);
+	rows[2 * (size_t) v + 1] = make_uint4(r[4], r[5], r[6], r[7]);
+}
+
 __global__ void max_kernel(const uint32_t *__restrict__ in, size_t n, uint32_t *out)
 {
 	uint32_t m = 0;
@@ -212,6 +228,13 @@ cudaError_t launch_fan_fill(const uint32_t *VT, const uint32_t *OT, const uint32
 {
 	if(!nv) return cudaSuccess;
 	fan_fill_kernel<<<(nv + 255) / 256, 256, 0, s>>>(VT, OT, EVT, nv, flags, off, fan);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_fan8(const uint32_t *off, const uint32_t *fan, uint32_t nv, uint4 *rows, cudaStream_t s)
+{
+	if(!nv) return cudaSuccess;
+	fan8_kernel<<<(nv + 255) / 256, 256, 0, s>>>(off, fan, nv, rows);
 	return cudaGetLastError();
 }
 

@@ -185,6 +185,11 @@ constexpr uint32_t FB = 8;
 template <bool CL, bool COH>
 __device__ __forceinline__ void take32(const Nb32 &a, const Nb32 &b, float &best, uint32_t &lab, const uint32_t *Co)
 {
+	// A triangle whose two neighbours are both no closer than the current best
+	// cannot improve it: the edge fallback is >= min(t0, t1), and a causal
+	// planar solution lies beyond both t0 and t1 (delta = p - t0 > 0, rounding
+	// can only matter when delta is within ~1e-6 edge of 0).  Skip the solve.
+	if(fminf(a.t, b.t) >= best) return;
 	const float p = update32(a, b);
 	if(p < best)
 	{
@@ -304,24 +309,70 @@ __device__ __forceinline__ Nb32 make_nb(float4 pu, float t, float4 pv, uint32_t 
 // registers, several loads in flight).  Returns the new (hi, lo) pair.
 constexpr uint32_t FC = 4;
 
+// (bh, bl) + x, exactly in double-float
+__device__ __forceinline__ float2 df_add(float bh, float bl, float x)
+{
+	const float s0 = bh + x;
+	const float bb = s0 - bh;
+	const float e = (bh - (s0 - bb)) + (x - bb) + bl;
+	const float h = s0 + e;
+	return make_float2(h, e - (h - s0));
+}
+
+// Vertices of valence above 8: the fan from the CSR lists, one neighbour at a time.
 template <bool CL, bool COH>
-__device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const float2 *Do, const uint32_t *Co,
-                                          uint32_t &lab)
+__device__ __noinline__ float2 relax32_csr(const FieldDev &F, uint32_t v, const float2 *Do, const uint32_t *Co,
+                                           uint32_t &lab, float2 vd, float4 pv)
 {
 	const uint32_t o0f = __ldg(F.off + v);
 	const uint32_t o1 = __ldg(F.off + v + 1) & FAN_MASK;
 	const uint32_t o0 = o0f & FAN_MASK;
-	const float2 vd = ld2<COH>(Do + v);
-	if(CL) lab = ld_d<uint32_t, COH>(Co + v);
-	if(o1 <= o0) return vd;
-	const uint32_t n = o1 - o0;
-	const float4 pv = __ldg(F.P + v);
+	const uint32_t n = o1 > o0 ? o1 - o0 : 0u;
+	if(!n) return vd;
 	const uint32_t *fan = F.fan + o0;
-	uint32_t u[FB];
+	float bh = vd.x, bl = vd.y;
+	if(bh == INFINITY)
+	{
+		float m = INFINITY;
+		for(uint32_t k = 0; k < n; k++) m = fminf(m, ld2<COH>(Do + __ldg(fan + k)).x);
+		bh = m == INFINITY ? 0.f : m;
+		bl = 0.f;
+	}
+	const float old_rel = vd.x == INFINITY ? INFINITY : 0.f;
+	float best = old_rel;
+	const uint32_t w0 = __ldg(fan);
+	const Nb32 first = make_nb(__ldg(F.P + w0), rel_to(ld2<COH>(Do + w0), bh, bl), pv, w0);
+	Nb32 last = first;
+	for(uint32_t e = 1; e < n; e++)
+	{
+		const uint32_t w = __ldg(fan + e);
+		const Nb32 cur = make_nb(__ldg(F.P + w), rel_to(ld2<COH>(Do + w), bh, bl), pv, w);
+		take32<CL, COH>(last, cur, best, lab, Co);
+		last = cur;
+	}
+	if(o0f & FAN_CLOSED) take32<CL, COH>(last, first, best, lab, Co);
+	if(!(best < old_rel)) return vd;
+	return df_add(bh, bl, best);
+}
+
+template <bool CL, bool COH>
+__device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const float2 *Do, const uint32_t *Co,
+                                          uint32_t &lab)
+{
+	// the fan row, the vertex's own distance and position: one memory trip
+	const uint4 ra = __ldg(F.fan8 + 2 * (size_t) v), rb = __ldg(F.fan8 + 2 * (size_t) v + 1);
+	const float2 vd = ld2<COH>(Do + v);
+	const float4 pv = __ldg(F.P + v);
+	if(CL) lab = ld_d<uint32_t, COH>(Co + v);
+	uint32_t u[FB] = {ra.x & FAN_MASK, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+	const bool closed = (ra.x & FAN_CLOSED) != 0 && ra.x != FAN8_EMPTY;
+	if(rb.w == FAN8_OVERFLOW) return relax32_csr<CL, COH>(F, v, Do, Co, lab, vd, pv);
+	uint32_t n = 0;
 #pragma unroll
-	for(uint32_t k = 0; k < FB; k++) u[k] = k < n ? __ldg(fan + k) : 0u;
+	for(uint32_t k = 0; k < FB; k++) n += (k == 0 ? ra.x : u[k]) != FAN8_EMPTY;
+	if(!n) return vd;
 	// base of the relative distances: the vertex itself, or (while it is INF)
-	// its smallest neighbour among the first FB
+	// its smallest neighbour
 	float bh = vd.x, bl = vd.y;
 	if(bh == INFINITY)
 	{
@@ -338,14 +389,14 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 #pragma unroll
 	for(uint32_t c = 0; c < FB; c += FC)
 	{
-		float4 pk[FC];
 		float2 dk[FC];
+		float4 pk[FC];
 #pragma unroll
 		for(uint32_t q = 0; q < FC; q++)
 			if(c + q < n)
 			{
-				pk[q] = __ldg(F.P + u[c + q]);
 				dk[q] = ld2<COH>(Do + u[c + q]);
+				pk[q] = __ldg(F.P + u[c + q]);
 			}
 #pragma unroll
 		for(uint32_t q = 0; q < FC; q++)
@@ -357,22 +408,9 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 				last = cur;
 			}
 	}
-	// valence above FB: the rest one neighbour at a time
-	for(uint32_t e = FB; e < n; e++)
-	{
-		const uint32_t w = __ldg(fan + e);
-		const Nb32 cur = make_nb(__ldg(F.P + w), rel_to(ld2<COH>(Do + w), bh, bl), pv, w);
-		take32<CL, COH>(last, cur, best, lab, Co);
-		last = cur;
-	}
-	if(o0f & FAN_CLOSED) take32<CL, COH>(last, first, best, lab, Co);
+	if(closed) take32<CL, COH>(last, first, best, lab, Co);
 	if(!(best < old_rel)) return vd;
-	// (bh, bl) + best, exactly in double-float
-	const float s0 = bh + best;
-	const float bb = s0 - bh;
-	const float e = (bh - (s0 - bb)) + (best - bb) + bl;
-	const float h = s0 + e;
-	return make_float2(h, e - (h - s0));
+	return df_add(bh, bl, best);
 }
 
 // Relax window vertex v of field F (buffers d -> d^1) and, if v is in the
@@ -593,7 +631,8 @@ __global__ void __launch_bounds__(NT, 3) ptp_kernel(GridArgs a)
 	uint32_t *id = ts + F + 1;
 	__shared__ uint32_t s_G;
 	const uint32_t lane = threadIdx.x & 31;
-	constexpr uint32_t TV = NT;  // window vertices per tile
+	constexpr uint32_t TV = 32;  // window vertices per tile: one warp's worth
+	const uint32_t warps = gridDim.x * (NT / 32), wid = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
 
 	if(threadIdx.x == 0) s_G = 0;
 	__syncthreads();
@@ -642,7 +681,7 @@ __global__ void __launch_bounds__(NT, 3) ptp_kernel(GridArgs a)
 		}
 		if(!total) break;
 		uint32_t *flags = a.notok + (step % 3) * F;
-		for(uint32_t k = blockIdx.x; k < total; k += gridDim.x)
+		for(uint32_t k = wid; k < total; k += warps)
 		{
 			uint32_t lo = 0, hi = G;  // last entry whose first tile <= k
 			while(hi - lo > 1)
@@ -654,7 +693,7 @@ __global__ void __launch_bounds__(NT, 3) ptp_kernel(GridArgs a)
 			const SchedSmem &x = fs[lo];
 			const uint32_t f = id[lo];
 			int bad = 0;
-			const uint32_t v = x.win_s + (k - ts[lo]) * TV + threadIdx.x;
+			const uint32_t v = x.win_s + (k - ts[lo]) * TV + lane;
 			if(v < x.win_e) bad = sweep_vertex<T, CL, true>(a.fields[f], x.d, v, x.chk_e);
 			// one atomic per warp that saw a failure, no block barrier per tile
 			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
@@ -797,6 +836,24 @@ __global__ void fill_kernel(CatArgs c)
 				F.fan[dst + (e - o0)] = iu ? iu - 1 : nr;
 			}
 			F.off[k] = dst | (o0f & FAN_CLOSED);
+			{
+				uint32_t r[8];
+				const uint32_t n = o1 - o0;
+				for(uint32_t q = 0; q < 8; q++)
+				{
+					uint32_t x = FAN8_EMPTY;
+					if(q < n)
+					{
+						const uint32_t iu = F.inv[F.m.fan[o0 + q]];
+						x = iu ? iu - 1 : nr;
+					}
+					r[q] = x;
+				}
+				if(n > 8) r[7] = FAN8_OVERFLOW;
+				if(n && (o0f & FAN_CLOSED)) r[0] |= FAN_CLOSED;
+				F.fan8[2 * (size_t) k] = make_uint4(r[0], r[1], r[2], r[3]);
+				F.fan8[2 * (size_t) k + 1] = make_uint4(r[4], r[5], r[6], r[7]);
+			}
 			F.P[k] = F.m.pos[v];
 			if(F.Pd)
 			{
@@ -824,6 +881,8 @@ __global__ void fill_kernel(CatArgs c)
 		else if(k == nr)
 		{
 			F.off[k] = c.cnt[g];
+			F.fan8[2 * (size_t) k] = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);
+			F.fan8[2 * (size_t) k + 1] = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);
 			F.P[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 			if(F.Pd)
 				for(int q = 0; q < 4; q++) F.Pd[4 * (size_t) k + q] = 0.0;

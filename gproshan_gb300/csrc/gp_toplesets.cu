@@ -11,10 +11,13 @@
 //
 // One CTA owns one field at a time (fields are taken from a queue), so a level
 // needs only CTA barriers:
-//   discover: atomicMin(key[u], pos << 20 | slot) for every unvisited u;
+//   discover: atomicMin(key[u], (pos << 20 | slot) + 1) for every link entry of
+//             the frontier (no visited test, see discover());
 //   emit:     frontier chunks in `sorted` order; each vertex counts the u
 //             whose key it holds, a block scan (carried across chunks) gives
 //             their positions, and the owners write them and set ring[u].
+// The frontier's link rows stay in registers between the two passes and the
+// frontier itself in shared memory, so a level costs two memory trips.
 #include <mutex>
 
 #include "gp_common.cuh"
@@ -25,34 +28,69 @@ namespace {
 
 constexpr int BT = 1024;  // threads of a BFS CTA
 
-// Count (and with EMIT write) the vertices owned by frontier position p.
-template <bool EMIT>
-__device__ __forceinline__ uint32_t own(const FieldDev &F, uint32_t p, uint32_t level, uint32_t out)
+// Frontier vertices whose link rows a thread keeps in registers between the
+// two passes of a level, and the shared-memory copy of the frontier.
+constexpr uint32_t KB = 2;
+constexpr uint32_t SF = BT * KB;
+
+__device__ __forceinline__ uint32_t slot_of(const uint4 &a, const uint4 &b, uint32_t q)
 {
-	const uint32_t v = ldcg(F.sorted + p);
-	const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
-	uint32_t c = 0;
-	for(uint32_t e = o0; e < o1; e++)
+	const uint32_t x = q == 0 ? a.x : q == 1 ? a.y : q == 2 ? a.z : q == 3 ? a.w
+	                 : q == 4 ? b.x : q == 5 ? b.y : q == 6 ? b.z : b.w;
+	return q == 0 && x != FAN8_EMPTY ? x & FAN_MASK : x;
+}
+
+// discover: key[u] = min over the frontier of (position << 20 | link slot) + 1.
+// No visited test is needed: a vertex met at an earlier level already holds a
+// smaller key (its discoverer sat at an earlier position), and the sources
+// hold key 0 (set when seeded), so the min leaves them unchanged; a key match
+// at emit time therefore means "unvisited and first met here".
+__device__ __forceinline__ void discover(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &ra, const uint4 &rb)
+{
+	if(rb.w == FAN8_OVERFLOW)
 	{
-		const uint32_t u = __ldg(F.m.fan + e);
-		const unsigned long long mine = ((unsigned long long) p << 20) | (e - o0);
-		if(ldcg(F.ring + u) == NIL && ldcg(F.key + u) == mine)
-		{
-			if(EMIT)
-			{
-				F.sorted[out + c] = u;
-				F.ring[u] = level + 1;
-			}
-			c++;
-		}
+		const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
+		for(uint32_t e = o0; e < o1; e++)
+			atomicMin(F.key + __ldg(F.m.fan + e), (((unsigned long long) p << 20) | (e - o0)) + 1);
+		return;
 	}
-	return c;
+#pragma unroll
+	for(uint32_t q = 0; q < 8; q++)
+	{
+		const uint32_t u = slot_of(ra, rb, q);
+		if(u != FAN8_EMPTY) atomicMin(F.key + u, (((unsigned long long) p << 20) | q) + 1);
+	}
+}
+
+// The vertices owned by frontier position p (key match), as a slot mask;
+// overflow rows report their count and are re-walked at emit time.
+__device__ __forceinline__ uint32_t owned(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &ra, const uint4 &rb,
+                                          uint32_t &count)
+{
+	uint32_t mask = 0;
+	count = 0;
+	if(rb.w == FAN8_OVERFLOW)
+	{
+		const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
+		for(uint32_t e = o0; e < o1; e++)
+			count += ldcg(F.key + __ldg(F.m.fan + e)) == ((((unsigned long long) p << 20) | (e - o0)) + 1);
+		return 0;
+	}
+#pragma unroll
+	for(uint32_t q = 0; q < 8; q++)
+	{
+		const uint32_t u = slot_of(ra, rb, q);
+		if(u != FAN8_EMPTY && ldcg(F.key + u) == (((unsigned long long) p << 20) | q) + 1) mask |= 1u << q;
+	}
+	count = __popc(mask);
+	return mask;
 }
 
 __global__ void __launch_bounds__(BT) bfs_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields,
                                                  uint32_t *queue)
 {
 	__shared__ uint32_t s_f;
+	__shared__ uint32_t sf[2][SF];  // frontier copies: current and next level
 	for(;;)
 	{
 		if(threadIdx.x == 0) s_f = atomicAdd(queue, 1u);
@@ -64,32 +102,99 @@ __global__ void __launch_bounds__(BT) bfs_kernel(FieldDev *fields, FieldState *s
 		if(!state[f].bfs_live) continue;  // no sources, or a source out of range
 
 		uint32_t level = 0, s = 0, e = F.ns;  // frontier = ring 0 = [0, ns)
+		uint32_t cur = 0;
+		bool in_smem = false;                 // ring 0 is read from `sorted`
 		for(;;)
 		{
-			for(uint32_t p = s + threadIdx.x; p < e; p += BT)
+			// pass 1: rows of the frontier (first KB chunks kept in registers), discover
+			uint4 ra[KB], rb[KB];
+			uint32_t vv[KB];
+#pragma unroll
+			for(uint32_t c = 0; c < KB; c++)
 			{
-				const uint32_t v = ldcg(F.sorted + p);
-				const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
-				for(uint32_t q = o0; q < o1; q++)
+				const uint32_t p = s + c * BT + threadIdx.x;
+				if(p < e)
 				{
-					const uint32_t u = __ldg(F.m.fan + q);
-					if(ldcg(F.ring + u) == NIL) atomicMin(F.key + u, ((unsigned long long) p << 20) | (q - o0));
+					vv[c] = in_smem ? sf[cur][p - s] : ldcg(F.sorted + p);
+					ra[c] = __ldg(F.m.fan8 + 2 * (size_t) vv[c]);
+					rb[c] = __ldg(F.m.fan8 + 2 * (size_t) vv[c] + 1);
+					discover(F, p, vv[c], ra[c], rb[c]);
 				}
 			}
+			for(uint32_t p = s + SF + threadIdx.x; p < e; p += BT)
+			{
+				const uint32_t v = ldcg(F.sorted + p);
+				discover(F, p, v, __ldg(F.m.fan8 + 2 * (size_t) v), __ldg(F.m.fan8 + 2 * (size_t) v + 1));
+			}
 			__syncthreads();
+			// pass 2: count, scan in frontier order (carried across chunks), emit
 			uint32_t carry = 0;
-			for(uint32_t base = s; base < e; base += BT)
+			for(uint32_t base = s, c = 0; base < e; base += BT, c++)
 			{
 				const uint32_t p = base + threadIdx.x;
-				const uint32_t c = p < e ? own<false>(F, p, level, 0) : 0u;
+				uint32_t v = 0, cnt = 0, mask = 0;
+				uint4 a = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY), b = a;
+				if(p < e)
+				{
+					if(c < KB)
+					{
+						// registers of pass 1 (the loops unroll, so c is a constant per copy)
+#pragma unroll
+						for(uint32_t k = 0; k < KB; k++)
+							if(k == c)
+							{
+								v = vv[k];
+								a = ra[k];
+								b = rb[k];
+							}
+					}
+					else
+					{
+						v = ldcg(F.sorted + p);
+						a = __ldg(F.m.fan8 + 2 * (size_t) v);
+						b = __ldg(F.m.fan8 + 2 * (size_t) v + 1);
+					}
+					mask = owned(F, p, v, a, b, cnt);
+				}
 				uint32_t tot;
-				const uint32_t ex = block_exclusive_scan<BT>(c, &tot);
-				if(c) own<true>(F, p, level, e + carry + ex);
+				const uint32_t ex = block_exclusive_scan<BT>(cnt, &tot);
+				if(cnt)
+				{
+					uint32_t o = carry + ex;
+					if(b.w == FAN8_OVERFLOW)
+					{
+						const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
+						for(uint32_t q = o0; q < o1; q++)
+						{
+							const uint32_t u = __ldg(F.m.fan + q);
+							if(ldcg(F.key + u) == (((unsigned long long) p << 20) | (q - o0)) + 1)
+							{
+								F.sorted[e + o] = u;
+								F.ring[u] = level + 1;
+								if(o < SF) sf[cur ^ 1][o] = u;
+								o++;
+							}
+						}
+					}
+					else
+#pragma unroll
+						for(uint32_t q = 0; q < 8; q++)
+							if(mask & (1u << q))
+							{
+								const uint32_t u = slot_of(a, b, q);
+								F.sorted[e + o] = u;
+								F.ring[u] = level + 1;
+								if(o < SF) sf[cur ^ 1][o] = u;
+								o++;
+							}
+				}
 				carry += tot;
 			}
 			__syncthreads();
 			if(!carry) break;
 			if(threadIdx.x == 0) F.limits[level + 2] = e + carry;
+			in_smem = carry <= SF;
+			cur ^= 1;
 			s = e;
 			e += carry;
 			level++;
@@ -99,6 +204,7 @@ __global__ void __launch_bounds__(BT) bfs_kernel(FieldDev *fields, FieldState *s
 			state[f].n_limits = level + 2;
 			state[f].bfs_live = 0;
 		}
+		__syncthreads();
 	}
 }
 
@@ -138,6 +244,7 @@ __global__ void bfs_seed_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 		const uint32_t v = F.src[s];
 		F.sorted[s] = v;
 		F.ring[v] = 0;
+		F.key[v] = 0;  // below every discovery key: a source is never re-discovered
 	}
 	F.limits[0] = 0;
 	F.limits[1] = F.ns;

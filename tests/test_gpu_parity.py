@@ -206,3 +206,44 @@ def test_one_cta_and_grid_paths_agree(gpu_ctx, maker, src, precision):
     b, _, sb = _capi.ptp(m, src, dtype=dt, opts=_capi.make_opts(precision, local_window=1))
     assert sa.n_iter == sb.n_iter and sa.relaxations == sb.relaxations
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("src", [[0, 1, 2], [64, 65, 128, 0], [5, 5, 6], [4095, 4094]])
+def test_toplesets_adjacent_and_repeated_sources(gpu_ctx, oracle_lib, src):
+    """Sources next to each other (and repeated) stay in ring 0 and keep the
+    reference's order: a source is never re-discovered from a neighbour."""
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.height_field(64, 3)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    r_o, s_o, l_o = oracle_lib.toplesets(om, src)
+    rings, srt, lim = _capi.toplesets(m, src)
+    assert np.array_equal(rings, r_o) and np.array_equal(lim, l_o) and np.array_equal(srt, s_o)
+
+
+def test_toplesets_high_valence_vertex(gpu_ctx, oracle_lib):
+    """A fan of more than 8 triangles (link read from the CSR lists)."""
+    from gproshan_gb300 import _capi
+    k = 13
+    ang = np.linspace(0, 2 * np.pi, k, endpoint=False)
+    ring1 = np.stack([np.cos(ang), np.sin(ang), np.zeros(k)], 1)
+    ring2 = 2.1 * np.stack([np.cos(ang + 0.2), np.sin(ang + 0.2), 0.1 * np.ones(k)], 1)
+    xyz = np.concatenate([[[0.0, 0.0, 0.3]], ring1, ring2])
+    tri = []
+    for i in range(k):
+        a, b = 1 + i, 1 + (i + 1) % k
+        c, d = 1 + k + i, 1 + k + (i + 1) % k
+        tri += [[0, a, b], [a, c, b], [b, c, d]]
+    tri = np.array(tri, np.uint32)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    for src in ([0], [1 + k], [3, 0]):
+        r_o, s_o, l_o = oracle_lib.toplesets(om, src)
+        rings, srt, lim = _capi.toplesets(m, src)
+        assert np.array_equal(rings, r_o) and np.array_equal(lim, l_o) and np.array_equal(srt, s_o)
+        ref = oracle_lib.ptp(om, src, l_o, s_o)
+        d, _, st = _capi.ptp(m, src, dtype=np.float64, precision=_capi.GP_F64)
+        assert st.n_iter == ref["n_iter"] and np.array_equal(d, ref["dist"])
+        ref32 = oracle_lib.ptp(om, src, l_o, s_o, xyz=xyz.astype(np.float32).astype(np.float64))
+        d32, _, _ = _capi.ptp(m, src)
+        assert oracle_lib.max_rel_err(d32, ref32["dist"]) <= REL_TOL_F32
