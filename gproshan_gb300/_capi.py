@@ -41,7 +41,7 @@ class GPError(RuntimeError):
 class gp_ptp_opts(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("max_iter", C.c_uint32), ("tol", C.c_double),
                 ("threads", C.c_uint32), ("ctas", C.c_uint32), ("local_window", C.c_uint32),
-                ("round_coords", C.c_uint32), ("reserved", C.c_uint32 * 2)]
+                ("round_coords", C.c_uint32), ("schedule", C.c_uint32), ("reserved", C.c_uint32)]
 
 
 class gp_ptp_stats(C.Structure):
@@ -93,6 +93,14 @@ SIGNATURES = {
     "gp_ctx_step_trace": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_uint32)]),
     "gp_toplesets_noalloc": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_uint32,
                                        C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p]),
+    "gp_mlp_n_params": (C.c_uint32, []),
+    "gp_mlp_grad": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
+                              C.c_void_p]),
+    "gp_mlp_train": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32,
+                               C.c_float, C.c_void_p]),
+    "gp_mlp_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]),
+    "gp_ctx_set_cost_model": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gp_field_features": (C.c_int, [C.c_void_p, C.POINTER(gp_field), C.c_uint32, C.c_void_p]),
     "gp_fps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64,
                          C.c_double, C.POINTER(gp_ptp_opts), _u32p, C.POINTER(C.c_double),
                          C.POINTER(C.c_double)]),
@@ -264,9 +272,14 @@ def toplesets(mesh: DeviceMesh, sources):
     return rings, srt[:lim[-1]].copy() if len(lim) else srt[:0].copy(), lim
 
 
+GP_SCHED_REACTIVE = 0
+GP_SCHED_LEARNED = 1
+
+
 def make_opts(precision: int = GP_F32, max_iter: int = 0, tol: float = 0.0, ctas: int = 0,
-              local_window: int = 0, round_coords: bool = False) -> gp_ptp_opts:
+              local_window: int = 0, round_coords: bool = False, schedule: int = GP_SCHED_REACTIVE) -> gp_ptp_opts:
     o = gp_ptp_opts()
+    o.schedule = schedule
     o.round_coords = int(bool(round_coords))
     o.precision = precision
     o.max_iter = max_iter
@@ -299,7 +312,8 @@ def ptp(mesh: DeviceMesh, sources, limits=None, sorted_=None, dtype=np.float32, 
 
 
 def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP_F32, ctas: int = 0,
-              with_stats: bool = True, local_window: int = 0, round_coords: bool = False):
+              with_stats: bool = True, local_window: int = 0, round_coords: bool = False,
+              schedule: int = GP_SCHED_REACTIVE):
     """Solve many fields together (host arrays).  Returns (dists, stats, seconds)."""
     n = len(sources_list)
     out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
@@ -319,7 +333,8 @@ def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP
         fields[k].clusters = None
         fields[k].stats = C.addressof(stats[k]) if with_stats else None
     sec = C.c_double(0)
-    opts = make_opts(precision, ctas=ctas, local_window=local_window, round_coords=round_coords)
+    opts = make_opts(precision, ctas=ctas, local_window=local_window, round_coords=round_coords,
+                     schedule=schedule)
     st = lib().gp_ptp_batch(ctx.handle, fields, n, C.byref(opts), out_t, 0, C.byref(sec))
     ctx.check(st, "gp_ptp_batch")
     return dists, stats, sec.value
@@ -346,3 +361,64 @@ def fps(mesh: DeviceMesh, n: int, seeds=(0,), radio: float = 0.0, precision=GP_F
                       C.byref(opts), C.byref(n_out), C.byref(md), C.byref(sec))
     mesh.ctx.check(st, "gp_fps")
     return s[:n_out.value].copy(), md.value, sec.value
+
+
+# ---- sweep-cost model (3-layer MLP) ----------------------------------------
+MLP_IN = 16
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def mlp_n_params() -> int:
+    return int(lib().gp_mlp_n_params())
+
+
+def mlp_grad(ctx: Context, X, T, params):
+    """(grads, loss) of the mean squared error, FP32 kernels."""
+    X, T, p = _f32(X), _f32(T), _f32(params)
+    g = np.empty(mlp_n_params(), np.float32)
+    loss = C.c_float(0)
+    ctx.check(lib().gp_mlp_grad(ctx.handle, _ptr(X), _ptr(T), len(X), _ptr(p), _ptr(g), C.byref(loss)),
+              "gp_mlp_grad")
+    return g, float(loss.value)
+
+
+def mlp_train(ctx: Context, X, T, params, epochs: int, lr: float):
+    """Full-batch Adam on the GPU; returns (params, losses)."""
+    X, T = _f32(X), _f32(T)
+    p = _f32(params).copy()
+    losses = np.empty(epochs, np.float32)
+    ctx.check(lib().gp_mlp_train(ctx.handle, _ptr(X), _ptr(T), len(X), _ptr(p), epochs, float(lr),
+                                 _ptr(losses)), "gp_mlp_train")
+    return p, losses
+
+
+def mlp_infer(ctx: Context, X, params, bf16: bool = True):
+    X, p = _f32(X), _f32(params)
+    Y = np.empty((len(X), 2), np.float32)
+    ctx.check(lib().gp_mlp_infer(ctx.handle, _ptr(X), len(X), _ptr(p), _ptr(Y), int(bool(bf16))),
+              "gp_mlp_infer")
+    return Y
+
+
+def set_cost_model(ctx: Context, params):
+    p = None if params is None else _f32(params)
+    ctx.check(lib().gp_ctx_set_cost_model(ctx.handle, _ptr(p)), "gp_ctx_set_cost_model")
+
+
+def field_features(ctx: Context, meshes, sources_list):
+    """features[n][MLP_IN] of each field (toplesets on the GPU, no sweep)."""
+    n = len(sources_list)
+    fields = (gp_field * n)()
+    keep = []
+    for k in range(n):
+        src = _u32(sources_list[k])
+        keep.append(src)
+        fields[k].mesh = meshes[k].handle
+        fields[k].sources = src.ctypes.data
+        fields[k].n_sources = len(src)
+    out = np.empty((n, MLP_IN), np.float32)
+    ctx.check(lib().gp_field_features(ctx.handle, fields, n, _ptr(out)), "gp_field_features")
+    return out

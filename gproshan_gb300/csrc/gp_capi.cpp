@@ -10,6 +10,7 @@
 #include <vector>
 
 #include "gp_internal.h"
+#include "gp_mlp.h"
 
 namespace gp {
 // launchers defined in the .cu files and not in gp_internal.h's first list
@@ -28,9 +29,14 @@ cudaError_t launch_normalize(void *dist, bool f64, uint64_t n, unsigned long lon
 int ptp_threads();
 int ptp_local_max_ctas(int device, bool f64, bool clusters);
 cudaError_t launch_classify(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
-                            cudaStream_t s);
+                            const uint32_t *pred_big, cudaStream_t s);
 cudaError_t launch_ptp_local(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
-                             uint32_t ctas, uint32_t local_window, bool f64, bool clusters, cudaStream_t s);
+                             uint32_t ctas, uint32_t local_window, const uint32_t *perm, bool f64, bool clusters,
+                             cudaStream_t s);
+cudaError_t launch_field_features(const FieldDev *fields, const FieldState *state, uint32_t n_fields, float *out,
+                                  cudaStream_t s);
+cudaError_t launch_plan(const FieldDev *fields, const FieldState *state, uint32_t n_fields, const float *pred,
+                        uint32_t local_window, uint32_t *pred_big, float *cost, uint32_t *perm, cudaStream_t s);
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
                        cudaStream_t s);
@@ -57,6 +63,7 @@ struct gp_ctx {
 	int ptp_ctas[4] = {0, 0, 0, 0};
 	int local_ctas[4] = {0, 0, 0, 0};
 	uint32_t grid_ctas = 0;    // CTAs of the last grid launch
+	float *model = nullptr;    // cost-model parameters (device), or null
 };
 
 struct gp_mesh {
@@ -166,7 +173,7 @@ struct Req {
 	gp_ptp_stats *stats;
 };
 
-enum class Stage { toplesets, ptp };
+enum class Stage { toplesets, features, ptp };
 
 struct TopOut {  // host outputs of gp_toplesets
 	uint32_t *rings;
@@ -190,7 +197,7 @@ gp_status map_dev_err(gp_ctx *ctx, uint32_t err, const char *where)
 }
 
 gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts, gp_dtype out_type,
-              bool src_dev, bool out_dev, Stage stage, const TopOut *top, double *seconds)
+              bool src_dev, bool out_dev, Stage stage, const TopOut *top, double *seconds, float *features = nullptr)
 {
 	if(!ctx) return GP_ERR_INVALID_ARG;
 	if(!F) return GP_OK;
@@ -281,6 +288,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_sync = cv.add<GridSync>(2), o_base = cv.add<uint32_t>(F + 1), o_vbase = cv.add<uint32_t>(F + 1);
 	const size_t o_queue = cv.add<uint32_t>(4);
 	const size_t o_notok = cv.add<uint32_t>(3 * (size_t) F), o_bar = cv.add<uint32_t>(4);
+	const size_t o_feat = cv.add<float>((size_t) F * MLP_IN), o_pred = cv.add<float>((size_t) F * MLP_OUT);
+	const size_t o_pbig = cv.add<uint32_t>(F), o_cost = cv.add<float>(F), o_perm = cv.add<uint32_t>(F);
 	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
 	const size_t o_sorted = cv.add<uint32_t>(tot), o_lim = cv.add<uint32_t>(tot), o_inv = cv.add<uint32_t>(tot);
 	size_t o_cnt = 0, o_scan = 0, o_P = 0, o_Pd = 0, o_off = 0, o_fan = 0, o_D0 = 0, o_D1 = 0, o_C0 = 0, o_C1 = 0;
@@ -435,6 +444,13 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		cs.launches += (vtot ? 1 : 0) + 2;
 	}
 	GP_CUDA(ctx, cudaEventRecord(ctx->ph[1], s));
+	const bool learned = stage == Stage::ptp && o.schedule == GP_SCHED_LEARNED && ctx->model;
+	float *dfeat = reinterpret_cast<float *>(P(o_feat));
+	if(stage == Stage::features || learned)
+	{
+		GP_CUDA(ctx, launch_field_features(dF, dS, F, dfeat, s));
+		cs.launches += 1;
+	}
 	if(stage == Stage::ptp)
 	{
 		GP_CUDA(ctx, launch_renumber_batch(dF, dS, dBase, F, (uint32_t) tot, reinterpret_cast<uint32_t *>(P(o_cnt)),
@@ -443,9 +459,19 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		GP_CUDA(ctx, cudaEventRecord(ctx->ph[2], s));
 		const int kv = (f64 ? 2 : 0) + (clusters ? 1 : 0);
 		const uint32_t lw = o.local_window ? o.local_window : 4096u;
-		GP_CUDA(ctx, launch_classify(dF, dS, F, lw, s));
+		uint32_t *pbig = nullptr, *perm = nullptr;
+		if(learned)
+		{
+			pbig = reinterpret_cast<uint32_t *>(P(o_pbig));
+			perm = reinterpret_cast<uint32_t *>(P(o_perm));
+			float *pred = reinterpret_cast<float *>(P(o_pred));
+			GP_CUDA(ctx, mlp_infer_bf16_device(ctx->model, dfeat, (int) F, pred, s));
+			GP_CUDA(ctx, launch_plan(dF, dS, F, pred, lw, pbig, reinterpret_cast<float *>(P(o_cost)), perm, s));
+			cs.launches += 2;
+		}
+		GP_CUDA(ctx, launch_classify(dF, dS, F, lw, pbig, s));
 		GP_CUDA(ctx, launch_ptp_local(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_queue)),
-		                              (uint32_t) ctx->local_ctas[kv], lw, f64, clusters, s));
+		                              (uint32_t) ctx->local_ctas[kv], lw, perm, f64, clusters, s));
 		GP_CUDA(ctx, cudaEventRecord(ctx->ph[3], s));
 		const int maxc = ptp_max_ctas(ctx->device, f64, clusters, F);
 		uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
@@ -528,6 +554,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			reqs[f].stats->seconds = ms * 1e-3;
 		}
 
+	if(stage == Stage::features && features)
+		GP_CUDA(ctx, cudaMemcpy(features, dfeat, sizeof(float) * F * MLP_IN, cudaMemcpyDeviceToHost));
 	if(stage == Stage::toplesets && top)
 	{
 		const Req &r = reqs[0];
@@ -628,6 +656,7 @@ void gp_ctx_destroy(gp_ctx *ctx)
 	if(ctx->ws) cudaFree(ctx->ws);
 	if(ctx->pin) cudaFreeHost(ctx->pin);
 	if(ctx->steps) cudaFree(ctx->steps);
+	if(ctx->model) cudaFree(ctx->model);
 	if(ctx->ev0) cudaEventDestroy(ctx->ev0);
 	if(ctx->ev1) cudaEventDestroy(ctx->ev1);
 	for(int k = 0; k < 6; k++)
@@ -645,6 +674,7 @@ gp_status gp_ctx_step_trace(gp_ctx *ctx, uint32_t cap, uint64_t *out, uint32_t *
 	{
 		// (re)arm: record up to cap steps of the following calls' grid launches
 		if(ctx->steps) cudaFree(ctx->steps);
+	if(ctx->model) cudaFree(ctx->model);
 		ctx->steps = nullptr;
 		ctx->steps_cap = 0;
 		if(cap)
@@ -775,7 +805,7 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 	const size_t t_vt = tc.add<uint32_t>(nhe), t_ot = tc.add<uint32_t>(nhe), t_evt = tc.add<uint32_t>(nv);
 	const size_t t_cnt = tc.add<uint32_t>(nv + 1), t_flags = tc.add<uint32_t>(nv);
 	const size_t t_scan = tc.add<uint32_t>(scan_tmp_words(nv)), t_xyz = tc.add<double>(3 * (size_t) nv);
-	const size_t t_err = tc.add<uint32_t>(4);
+	const size_t t_err = tc.add<uint32_t>(4), t_acc = tc.add<double>(8);
 	gp_status st = ensure_ws(ctx, tc.off);
 	if(st != GP_OK) return st;
 	char *T = static_cast<char *>(ctx->ws);
@@ -831,7 +861,22 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 	if(e == cudaSuccess)
 		e = launch_pos_convert(reinterpret_cast<double *>(T + t_xyz), nv, const_cast<float4 *>(m->dev.pos),
 		                       const_cast<double *>(m->dev.posd), s);
+	double acc[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+	double *dacc = reinterpret_cast<double *>(T + t_acc);
+	if(e == cudaSuccess) e = cudaMemsetAsync(dacc, 0, sizeof(acc), s);
+	if(e == cudaSuccess) e = launch_mesh_stats(dvt, dot, m->dev.pos, nf, dacc, s);
+	if(e == cudaSuccess) e = cudaMemcpyAsync(acc, dacc, sizeof(acc), cudaMemcpyDeviceToHost, s);
 	if(e == cudaSuccess) e = cudaStreamSynchronize(s);
+	if(e == cudaSuccess)
+	{
+		const double ne = std::max(acc[4], 1.0), mean = acc[0] / ne, var = std::max(acc[1] / ne - mean * mean, 0.0);
+		const double gm = acc[2] / ne, gvar = std::max(acc[3] / ne - gm * gm, 0.0);
+		m->dev.stats[0] = (float) std::log(std::max(mean, 1e-30));
+		m->dev.stats[1] = (float) (mean > 0 ? std::sqrt(var) / mean : 0.0);
+		m->dev.stats[2] = (float) std::sqrt(gvar);
+		m->dev.stats[3] = (float) (nf ? acc[5] / nf : 0.0);
+		m->dev.stats[4] = (float) (acc[7] > 0 ? acc[6] / acc[7] : 0.0);
+	}
 	if(e != cudaSuccess)
 	{
 		set_err(ctx, "mesh upload: %s", cudaGetErrorString(e));
@@ -894,6 +939,118 @@ gp_status gp_ptp_batch(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, c
 		total += sec;
 	}
 	if(seconds) *seconds = total;
+	return GP_OK;
+}
+
+uint32_t gp_mlp_n_params(void) { return (uint32_t) MLP_NPARAM; }
+
+gp_status gp_ctx_set_cost_model(gp_ctx *ctx, const float *params)
+{
+	if(!ctx) return GP_ERR_INVALID_ARG;
+	if(!params)
+	{
+		if(ctx->model) cudaFree(ctx->model);
+		ctx->model = nullptr;
+		return GP_OK;
+	}
+	if(!ctx->model) GP_CUDA(ctx, cudaMalloc(reinterpret_cast<void **>(&ctx->model), sizeof(float) * MLP_NPARAM));
+	GP_CUDA(ctx, cudaMemcpy(ctx->model, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice));
+	return GP_OK;
+}
+
+gp_status gp_field_features(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, float *features)
+{
+	if(!ctx || !features || (n_fields && !fields)) return GP_ERR_INVALID_ARG;
+	std::vector<Req> reqs(n_fields);
+	for(uint32_t f = 0; f < n_fields; f++)
+		reqs[f] = Req{fields[f].mesh, fields[f].sources, fields[f].n_sources, nullptr, 0, nullptr, nullptr, nullptr,
+		              nullptr};
+	return run(ctx, reqs.data(), n_fields, nullptr, GP_F32, false, false, Stage::features, nullptr, nullptr, features);
+}
+
+namespace {
+
+// Device buffers of one MLP call inside the context workspace.
+struct MlpBufs {
+	float *X, *T, *P, *G, *M1, *M2, *work, *Y, *loss;
+};
+
+gp_status mlp_bufs(gp_ctx *ctx, uint32_t n, MlpBufs &b, uint32_t epochs = 0)
+{
+	Carve c;
+	const size_t oX = c.add<float>((size_t) n * MLP_IN), oT = c.add<float>((size_t) n * MLP_OUT);
+	const size_t oP = c.add<float>(MLP_NPARAM), oG = c.add<float>(MLP_NPARAM), oM1 = c.add<float>(MLP_NPARAM),
+	             oM2 = c.add<float>(MLP_NPARAM), oW = c.add<float>(mlp_workspace_floats((int) n)),
+	             oY = c.add<float>((size_t) n * MLP_OUT), oL = c.add<float>(4 + (size_t) epochs);
+	gp_status st = ensure_ws(ctx, c.off);
+	if(st != GP_OK) return st;
+	char *W = static_cast<char *>(ctx->ws);
+	b = MlpBufs{reinterpret_cast<float *>(W + oX), reinterpret_cast<float *>(W + oT), reinterpret_cast<float *>(W + oP),
+	            reinterpret_cast<float *>(W + oG), reinterpret_cast<float *>(W + oM1), reinterpret_cast<float *>(W + oM2),
+	            reinterpret_cast<float *>(W + oW), reinterpret_cast<float *>(W + oY), reinterpret_cast<float *>(W + oL)};
+	return GP_OK;
+}
+
+} // namespace
+
+gp_status gp_mlp_grad(gp_ctx *ctx, const float *X, const float *T, uint32_t n, const float *params, float *grads,
+                      float *loss)
+{
+	if(!ctx || !X || !T || !n || !params || !grads || !loss) return GP_ERR_INVALID_ARG;
+	MlpBufs b;
+	gp_status st = mlp_bufs(ctx, n, b);
+	if(st != GP_OK) return st;
+	cudaStream_t s = ctx->stream;
+	GP_CUDA(ctx, cudaMemcpyAsync(b.X, X, sizeof(float) * n * MLP_IN, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(b.T, T, sizeof(float) * n * MLP_OUT, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(b.P, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, mlp_grad_device(b.P, b.X, b.T, (int) n, b.work, b.G, b.loss, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(grads, b.G, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(loss, b.loss, sizeof(float), cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
+	return GP_OK;
+}
+
+gp_status gp_mlp_train(gp_ctx *ctx, const float *X, const float *T, uint32_t n, float *params, uint32_t epochs,
+                       float lr, float *losses)
+{
+	if(!ctx || !X || !T || !n || !params) return GP_ERR_INVALID_ARG;
+	MlpBufs b;
+	gp_status st = mlp_bufs(ctx, n, b, epochs);
+	if(st != GP_OK) return st;
+	cudaStream_t s = ctx->stream;
+	GP_CUDA(ctx, cudaMemcpyAsync(b.X, X, sizeof(float) * n * MLP_IN, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(b.T, T, sizeof(float) * n * MLP_OUT, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(b.P, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemsetAsync(b.M1, 0, sizeof(float) * MLP_NPARAM, s));
+	GP_CUDA(ctx, cudaMemsetAsync(b.M2, 0, sizeof(float) * MLP_NPARAM, s));
+	float *dl = b.loss + 4;  // per-epoch losses stay on the device until the end
+	for(uint32_t ep = 0; ep < epochs; ep++)
+	{
+		GP_CUDA(ctx, mlp_grad_device(b.P, b.X, b.T, (int) n, b.work, b.G, b.loss, s));
+		if(losses) GP_CUDA(ctx, cudaMemcpyAsync(dl + ep, b.loss, sizeof(float), cudaMemcpyDeviceToDevice, s));
+		GP_CUDA(ctx, mlp_adam_device(b.P, b.G, b.M1, b.M2, lr, (int) ep + 1, s));
+	}
+	GP_CUDA(ctx, cudaMemcpyAsync(params, b.P, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToHost, s));
+	if(losses && epochs)
+		GP_CUDA(ctx, cudaMemcpyAsync(losses, dl, sizeof(float) * epochs, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
+	return GP_OK;
+}
+
+gp_status gp_mlp_infer(gp_ctx *ctx, const float *X, uint32_t n, const float *params, float *Y, int bf16)
+{
+	if(!ctx || !X || !n || !params || !Y) return GP_ERR_INVALID_ARG;
+	MlpBufs b;
+	gp_status st = mlp_bufs(ctx, n, b);
+	if(st != GP_OK) return st;
+	cudaStream_t s = ctx->stream;
+	GP_CUDA(ctx, cudaMemcpyAsync(b.X, X, sizeof(float) * n * MLP_IN, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(b.P, params, sizeof(float) * MLP_NPARAM, cudaMemcpyHostToDevice, s));
+	if(bf16) GP_CUDA(ctx, mlp_infer_bf16_device(b.P, b.X, (int) n, b.Y, s));
+	else GP_CUDA(ctx, mlp_forward_f32_device(b.P, b.X, (int) n, b.work, b.Y, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(Y, b.Y, sizeof(float) * n * MLP_OUT, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
 	return GP_OK;
 }
 

@@ -48,6 +48,11 @@ struct MeshDev {
 	uint32_t n_fan;
 	uint32_t max_fan;        // largest per-vertex entry count
 	uint32_t pad;
+	// geometry statistics (cost-model features): log mean edge, edge-length
+	// coefficient of variation, std of log edge length, obtuse-triangle
+	// fraction, mean (1 - cos) of dihedral angles
+	float stats[5];
+	float pad2[3];
 };
 
 // Buffers of one field (one source set on one mesh) on the device.
@@ -134,6 +139,12 @@ int toplesets_max_ctas(int device);
 // gp_ptp.cu
 int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields);
 cudaError_t launch_argmax_abs(const void *dist, bool f64, uint32_t n, unsigned long long *out,
+                              cudaStream_t s);
+
+// gp_mesh.cu: sums for the geometry statistics (8 doubles, zeroed by the caller):
+// [0] sum l, [1] sum l^2, [2] sum log l, [3] sum (log l)^2, [4] edges,
+// [5] obtuse faces, [6] sum (1 - cos dihedral), [7] interior edges
+cudaError_t launch_mesh_stats(const uint32_t *VT, const uint32_t *OT, const float4 *pos, uint32_t nf, double *acc,
                               cudaStream_t s);
 
 // gp_capi.cpp: a mesh's device arrays and the device that holds them

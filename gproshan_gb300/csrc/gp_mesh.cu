@@ -93,6 +93,59 @@ __global__ void fan8_kernel(const uint32_t *__restrict__ off, const uint32_t *__
 	rows[2 * (size_t) v + 1] = make_uint4(r[4], r[5], r[6], r[7]);
 }
 
+// Per face: its three edge lengths (each edge counted from both sides, so
+// every interior edge twice: the averages are unaffected), whether it is
+// obtuse, and for each interior edge the dihedral deviation 1 - n1.n2.
+__global__ void mesh_stats_kernel(const uint32_t *__restrict__ VT, const uint32_t *__restrict__ OT,
+                                  const float4 *__restrict__ pos, uint32_t nf, double *acc)
+{
+	double l1 = 0, l2 = 0, g1 = 0, g2 = 0, ne = 0, obt = 0, dih = 0, ni = 0;
+	for(uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nf; t += gridDim.x * blockDim.x)
+	{
+		const float4 a = pos[VT[3 * t]], b = pos[VT[3 * t + 1]], c = pos[VT[3 * t + 2]];
+		const float3 e0 = make_float3(b.x - a.x, b.y - a.y, b.z - a.z);
+		const float3 e1 = make_float3(c.x - b.x, c.y - b.y, c.z - b.z);
+		const float3 e2 = make_float3(a.x - c.x, a.y - c.y, a.z - c.z);
+		const float q[3] = {e0.x * e0.x + e0.y * e0.y + e0.z * e0.z, e1.x * e1.x + e1.y * e1.y + e1.z * e1.z,
+		                    e2.x * e2.x + e2.y * e2.y + e2.z * e2.z};
+		for(int k = 0; k < 3; k++)
+			if(q[k] > 0.f)
+			{
+				const double l = sqrt((double) q[k]), g = log(l);
+				l1 += l;
+				l2 += l * l;
+				g1 += g;
+				g2 += g * g;
+				ne += 1;
+			}
+		const float qm = fmaxf(q[0], fmaxf(q[1], q[2]));
+		obt += 2.f * qm > q[0] + q[1] + q[2];  // q_max > q_other1 + q_other2
+		float3 n = make_float3(e0.y * e1.z - e0.z * e1.y, e0.z * e1.x - e0.x * e1.z, e0.x * e1.y - e0.y * e1.x);
+		const float nn = sqrtf(n.x * n.x + n.y * n.y + n.z * n.z);
+		for(int k = 0; k < 3; k++)
+		{
+			const uint32_t o = OT[3 * t + k];
+			if(o == NIL || o / 3 < t || nn <= 0.f) continue;  // each interior edge once
+			const uint32_t u = o / 3;
+			const float4 A = pos[VT[3 * u]], B = pos[VT[3 * u + 1]], C = pos[VT[3 * u + 2]];
+			const float3 f0 = make_float3(B.x - A.x, B.y - A.y, B.z - A.z);
+			const float3 f1 = make_float3(C.x - B.x, C.y - B.y, C.z - B.z);
+			const float3 m = make_float3(f0.y * f1.z - f0.z * f1.y, f0.z * f1.x - f0.x * f1.z, f0.x * f1.y - f0.y * f1.x);
+			const float mm = sqrtf(m.x * m.x + m.y * m.y + m.z * m.z);
+			if(mm <= 0.f) continue;
+			dih += 1.0 - (double) ((n.x * m.x + n.y * m.y + n.z * m.z) / (nn * mm));
+			ni += 1;
+		}
+	}
+	double v[8] = {l1, l2, g1, g2, ne, obt, dih, ni};
+	for(int k = 0; k < 8; k++)
+	{
+		double x = v[k];
+		for(int o = 16; o; o >>= 1) x += __shfl_xor_sync(0xffffffffu, x, o);
+		if((threadIdx.x & 31) == 0) atomicAdd(acc + k, x);
+	}
+}
+
 __global__ void max_kernel(const uint32_t *__restrict__ in, size_t n, uint32_t *out)
 {
 	uint32_t m = 0;
@@ -235,6 +288,15 @@ cudaError_t launch_fan8(const uint32_t *off, const uint32_t *fan, uint32_t nv, u
 {
 	if(!nv) return cudaSuccess;
 	fan8_kernel<<<(nv + 255) / 256, 256, 0, s>>>(off, fan, nv, rows);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_mesh_stats(const uint32_t *VT, const uint32_t *OT, const float4 *pos, uint32_t nf, double *acc,
+                              cudaStream_t s)
+{
+	if(!nf) return cudaSuccess;
+	const unsigned nb = (unsigned) std::min<uint32_t>((nf + 255) / 256, 152 * 8);
+	mesh_stats_kernel<<<nb, 256, 0, s>>>(VT, OT, pos, nf, acc);
 	return cudaGetLastError();
 }
 

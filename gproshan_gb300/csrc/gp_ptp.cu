@@ -21,6 +21,7 @@
 #include <type_traits>
 
 #include "gp_common.cuh"
+#include "gp_mlp.h"
 
 namespace gp {
 
@@ -455,7 +456,8 @@ labels:
 // record the largest window its schedule could open, max_j limits[j] -
 // limits[j/2] (statistics).  Every field starts on one CTA.
 // ---------------------------------------------------------------------------
-__global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window)
+__global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
+                                const uint32_t *pred_big)
 {
 	const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
 	if(warp >= n_fields) return;
@@ -479,9 +481,100 @@ __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 		st.live = 0;
 		st.relax = 0;
 		st.max_iter = F.max_iter ? F.max_iter : (nl << 1);
+		st.n_limits = nl;
+		// a field the cost model expects to outgrow one CTA starts on the grid
+		// launch right away (its first sweep opened here)
+		if(pred_big && pred_big[warp] && nl >= 3)
+		{
+			open_sweep(F, st, true);
+			st.big = st.live;
+		}
 	}
 	(void) local_window;
 }
+
+// ---------------------------------------------------------------------------
+// Cost-model features of every field (one warp per field), from its toplesets
+// and its mesh's geometry statistics; the 16 values of GP_MLP_IN.
+// ---------------------------------------------------------------------------
+__global__ void field_features_kernel(const FieldDev *fields, const FieldState *state, uint32_t n_fields, float *out)
+{
+	const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, lane = threadIdx.x & 31;
+	if(warp >= n_fields) return;
+	const FieldDev &F = fields[warp];
+	const uint32_t nl = state[warp].n_limits;
+	const uint32_t L = nl ? nl - 1 : 0;
+	const uint32_t *lim = F.limits;
+	uint32_t rmax = 0, amax = 0, bound = 0;
+	for(uint32_t k = lane; k < L; k += 32)
+	{
+		const uint32_t r = lim[k + 1] - lim[k];
+		if(r > rmax) { rmax = r; amax = k; }
+	}
+	for(uint32_t j = 2 + lane; j < nl; j += 32) bound = max(bound, lim[j] - lim[j >> 1]);
+	for(int o = 16; o; o >>= 1)
+	{
+		const uint32_t r2 = __shfl_xor_sync(0xffffffffu, rmax, o), a2 = __shfl_xor_sync(0xffffffffu, amax, o);
+		if(r2 > rmax || (r2 == rmax && a2 < amax)) { rmax = r2; amax = a2; }
+		bound = max(bound, __shfl_xor_sync(0xffffffffu, bound, o));
+	}
+	if(lane) return;
+	const uint32_t nr = nl ? lim[nl - 1] : 0;
+	auto ring = [&](uint32_t k) { return k < L ? (float) (lim[k + 1] - lim[k]) : 0.f; };
+	const float Lf = (float) max(L, 1u);
+	float *x = out + (size_t) warp * MLP_IN;
+	x[0] = logf((float) max(F.m.nv, 1u));
+	x[1] = logf(Lf);
+	x[2] = logf((float) max(F.ns, 1u));
+	x[3] = logf((float) max(rmax, 1u));
+	x[4] = logf(fmaxf((float) nr / Lf, 1.f));
+	x[5] = (float) amax / Lf;
+	x[6] = logf((float) bound + 1.f);
+	x[7] = logf(ring(L / 4) + 1.f);
+	x[8] = logf(ring(L / 2) + 1.f);
+	x[9] = logf(ring(3 * L / 4) + 1.f);
+	x[10] = F.m.stats[0];
+	x[11] = F.m.stats[1];
+	x[12] = F.m.stats[2];
+	x[13] = F.m.stats[3];
+	x[14] = F.m.stats[4];
+	x[15] = (float) nr / (float) max(F.m.nv, 1u);
+}
+
+// Predictions -> start mode and local queue order (one CTA).  Predicted
+// sweeps s = rings * exp(y0), relaxations r = vertices * exp(y1); a field
+// whose mean window r / s exceeds local_window starts on the grid launch; the
+// others are queued longest predicted chain first (s * ceil(window / LT)).
+__global__ void __launch_bounds__(1024) plan_kernel(const FieldDev *fields, const FieldState *state, uint32_t n_fields,
+                                                    const float *pred, uint32_t local_window, uint32_t lt,
+                                                    uint32_t *pred_big, float *cost, uint32_t *perm)
+{
+	for(uint32_t f = threadIdx.x; f < n_fields; f += blockDim.x)
+	{
+		const uint32_t nl = state[f].n_limits;
+		const float L = (float) (nl ? nl - 1 : 1);
+		const float sw = fmaxf(L * expf(pred[2 * f]), 1.f);
+		const float rx = (float) fields[f].m.nv * expf(pred[2 * f + 1]);
+		const float win = rx / sw;
+		const uint32_t big = nl >= 3 && win > (float) local_window;
+		const float c = sw * fmaxf(1.f, ceilf(win / (float) lt));
+		pred_big[f] = big;
+		cost[f] = big ? -1.f : (c == c ? c : 0.f);  // a NaN cost would break the ranking
+	}
+	__syncthreads();
+	for(uint32_t f = threadIdx.x; f < n_fields; f += blockDim.x)
+	{
+		const float c = cost[f];
+		uint32_t rank = 0;
+		for(uint32_t g = 0; g < n_fields; g++)
+		{
+			const float d = cost[g];
+			rank += d > c || (d == c && g < f);
+		}
+		perm[rank] = f;
+	}
+}
+
 
 // ---------------------------------------------------------------------------
 // One CTA sweeps one field (run_ptp_gpu's loop, src/cuda/geodesics_ptp.cu:
@@ -495,18 +588,22 @@ constexpr int LT = 512;
 
 template <typename T, bool CL>
 __global__ void __launch_bounds__(LT) ptp_local_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields,
-                                                       uint32_t *queue, uint32_t local_window)
+                                                       uint32_t *queue, uint32_t local_window, const uint32_t *perm)
 {
 	__shared__ uint32_t s_f;
 	for(;;)
 	{
-		if(threadIdx.x == 0) s_f = atomicAdd(queue, 1u);
+		if(threadIdx.x == 0)
+		{
+			const uint32_t q = atomicAdd(queue, 1u);
+			s_f = q < n_fields && perm ? perm[q] : q;
+		}
 		__syncthreads();
 		const uint32_t f = s_f;
 		__syncthreads();
 		if(f >= n_fields) return;
 		FieldState &gst = state[f];
-		if(gst.n_limits < 3) continue;
+		if(gst.n_limits < 3 || gst.big) continue;
 		const FieldDev &F = fields[f];
 		FieldState st = {};
 		st.i = 1;
@@ -1082,22 +1179,40 @@ int ptp_local_max_ctas(int device, bool f64, bool clusters)
 }
 
 cudaError_t launch_classify(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
-                            cudaStream_t s)
+                            const uint32_t *pred_big, cudaStream_t s)
 {
 	if(!n_fields) return cudaSuccess;
-	classify_kernel<<<(n_fields * 32 + 255) / 256, 256, 0, s>>>(fields, state, n_fields, local_window);
+	classify_kernel<<<(n_fields * 32 + 255) / 256, 256, 0, s>>>(fields, state, n_fields, local_window, pred_big);
 	return cudaGetLastError();
 }
 
-// queue: one word, zeroed here (the field ticket)
+// queue: one word, zeroed here (the field ticket); perm: null or the order
+// in which fields are taken
 cudaError_t launch_ptp_local(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
-                             uint32_t ctas, uint32_t local_window, bool f64, bool clusters, cudaStream_t s)
+                             uint32_t ctas, uint32_t local_window, const uint32_t *perm, bool f64, bool clusters,
+                             cudaStream_t s)
 {
 	cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
 	if(e != cudaSuccess) return e;
 	ctas = std::max<uint32_t>(1, std::min<uint32_t>(ctas, n_fields));
-	void *args[] = {&fields, &state, &n_fields, &queue, &local_window};
+	void *args[] = {&fields, &state, &n_fields, &queue, &local_window, &perm};
 	return cudaLaunchKernel(ptp_local_ptr(f64, clusters), dim3(ctas), dim3(LT), args, 0, s);
+}
+
+cudaError_t launch_field_features(const FieldDev *fields, const FieldState *state, uint32_t n_fields, float *out,
+                                  cudaStream_t s)
+{
+	if(!n_fields) return cudaSuccess;
+	field_features_kernel<<<(n_fields * 32 + 255) / 256, 256, 0, s>>>(fields, state, n_fields, out);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_plan(const FieldDev *fields, const FieldState *state, uint32_t n_fields, const float *pred,
+                        uint32_t local_window, uint32_t *pred_big, float *cost, uint32_t *perm, cudaStream_t s)
+{
+	if(!n_fields) return cudaSuccess;
+	plan_kernel<<<1, 1024, 0, s>>>(fields, state, n_fields, pred, local_window, LT, pred_big, cost, perm);
+	return cudaGetLastError();
 }
 
 cudaError_t launch_normalize(void *dist, bool f64, uint64_t n, unsigned long long *tmp, cudaStream_t s)

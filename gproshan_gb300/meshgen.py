@@ -111,19 +111,22 @@ def _grid_faces(nr: int, nc: int):
 
 
 def height_field(n: int = 2048, seed: int = 0, n_waves: int = 8, amp: float = 0.05,
-                 fmin: float = 1.0, fmax: float = 16.0):
-    """``n x n`` grid on [0,1]^2, z = sum of ``n_waves`` seeded sinusoids."""
+                 fmin: float = 1.0, fmax: float = 16.0, cols: int | None = None):
+    """``n x n`` grid on [0,1]^2 (``n x cols`` on [0,cols/n]x[0,1] when ``cols`` is
+    given: a strip), z = sum of ``n_waves`` seeded sinusoids."""
     rng = np.random.default_rng(seed)
     fx = rng.uniform(fmin, fmax, n_waves) * rng.choice([-1.0, 1.0], n_waves)
     fy = rng.uniform(fmin, fmax, n_waves) * rng.choice([-1.0, 1.0], n_waves)
     ph = rng.uniform(0.0, 2.0 * np.pi, n_waves)
+    nc = n if cols is None else int(cols)
     u = np.linspace(0.0, 1.0, n)
-    U, V = np.meshgrid(u, u, indexing="xy")  # row r -> y, column c -> x
+    uc = u if cols is None else np.arange(nc) / max(n - 1, 1)
+    U, V = np.meshgrid(uc, u, indexing="xy")  # row r -> y, column c -> x
     Z = np.zeros_like(U)
     for k in range(n_waves):
         Z += amp * np.sin(2.0 * np.pi * (fx[k] * U + fy[k] * V) + ph[k])
     xyz = np.stack([U.ravel(), V.ravel(), Z.ravel()], 1)
-    return xyz.astype(np.float64), _grid_faces(n, n)
+    return xyz.astype(np.float64), _grid_faces(n, nc)
 
 
 def torus(n_major: int = 400, n_minor: int = 2500, R: float = 1.0, r: float = 0.3,

@@ -114,8 +114,17 @@ typedef struct gp_ptp_opts {
 	                          swept by one CTA each; 0: default (4096) */
 	uint32_t round_coords; /* GP_F64 only: 1 = solve on the float-rounded coordinates
 	                          the GP_F32 path sees (an FP64 check of an FP32 run) */
-	uint32_t reserved[2];
+	uint32_t schedule;     /* GP_SCHED_REACTIVE (0) or GP_SCHED_LEARNED (1): see below */
+	uint32_t reserved;
 } gp_ptp_opts;
+
+/* Batch scheduling.  REACTIVE: every field starts on one CTA and moves to the
+ * grid-wide launch when a window outgrows local_window.  LEARNED: the context's
+ * cost model (gp_ctx_set_cost_model) predicts each field's sweeps and work from
+ * its toplesets; fields expected to outgrow one CTA start on the grid launch,
+ * the rest are taken longest-predicted-first.  Results are identical. */
+#define GP_SCHED_REACTIVE 0u
+#define GP_SCHED_LEARNED 1u
 
 typedef struct gp_ptp_stats {
 	uint32_t n_iter;       /* sweeps run */
@@ -224,6 +233,44 @@ gp_status gp_ctx_step_trace(gp_ctx *ctx, uint32_t cap, uint64_t *out, uint32_t *
 gp_status gp_toplesets_noalloc(const gp_mesh *mesh, const uint32_t *sources, uint32_t n_sources,
                                uint32_t *rings, uint32_t *sorted, uint32_t cap_sorted, uint32_t *limits,
                                uint32_t cap_limits, uint32_t *n_limits, void *stream);
+
+/* ------------------------------------------------------------------ */
+/* learned sweep-cost model                                            */
+/* ------------------------------------------------------------------ */
+/*
+ * A 3-layer MLP (GP_MLP_IN -> 64 -> 64 -> 2, ReLU) predicting, per field,
+ * log(sweeps / rings) and log(relaxations / vertices) from the field features
+ * of gp_field_features.  Trained on the GPU by the library's own FP32
+ * forward/backward/Adam kernels; evaluated with BF16 tensor-core inference.
+ * It only steers scheduling (where a field starts, the order fields are taken);
+ * results never depend on it.  No reference counterpart: gproshan runs a fixed
+ * convergence loop per field (src/cuda/geodesics_ptp.cu:206-229).
+ *
+ * Parameters: a flat float array of gp_mlp_n_params() values,
+ * W1[GP_MLP_IN][64] b1[64] W2[64][64] b2[64] W3[64][2] b3[2].
+ * All arrays below are host arrays.
+ */
+#define GP_MLP_IN 16
+uint32_t gp_mlp_n_params(void);
+/* One forward/backward pass of the mean squared error over n samples:
+ * X[n][GP_MLP_IN], T[n][2] -> grads[n_params], *loss. */
+gp_status gp_mlp_grad(gp_ctx *ctx, const float *X, const float *T, uint32_t n, const float *params,
+                      float *grads, float *loss);
+/* Full-batch Adam for `epochs` steps at learning rate lr; params updated in
+ * place; losses[epochs] (may be null) receives the loss before each step. */
+gp_status gp_mlp_train(gp_ctx *ctx, const float *X, const float *T, uint32_t n, float *params, uint32_t epochs,
+                       float lr, float *losses);
+/* Y[n][2] = MLP(X): bf16 != 0 uses the BF16 tensor-core kernel (FP32
+ * accumulation), else the FP32 kernels of training. */
+gp_status gp_mlp_infer(gp_ctx *ctx, const float *X, uint32_t n, const float *params, float *Y, int bf16);
+
+/* Install (params != null, gp_mlp_n_params() floats) or remove the cost model
+ * used by GP_SCHED_LEARNED on this context. */
+gp_status gp_ctx_set_cost_model(gp_ctx *ctx, const float *params);
+/* The GP_MLP_IN features of each field (toplesets computed on the GPU, no
+ * sweep): features[n_fields][GP_MLP_IN], host array.  The fields' dist,
+ * clusters and stats members are not used. */
+gp_status gp_field_features(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, float *features);
 
 /* normalize_ptp (src/geodesics_ptp.cpp:264-276) on a host array. */
 gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n);
