@@ -134,7 +134,7 @@ class ClockSampler:
 # --------------------------------------------------------------------------
 def run_gpu(args, rank, world, local):
     import torch
-    from gproshan_gb300 import _capi, build
+    from gproshan_gb300 import _capi, build, learned
 
     build.build()
     torch.cuda.set_device(local)
@@ -166,7 +166,12 @@ def run_gpu(args, rank, world, local):
         return arr
 
     dev_fields = field_array(True)
-    opts = _capi.make_opts(_capi.GP_F32)
+    sched = _capi.GP_SCHED_LEARNED if args.schedule == "learned" else _capi.GP_SCHED_REACTIVE
+    if sched == _capi.GP_SCHED_LEARNED:
+        learned.install(ctx)
+    gk = {"auto": _capi.GP_GRID_AUTO, "lockstep": _capi.GP_GRID_LOCKSTEP, "queue": _capi.GP_GRID_QUEUE}
+    opts = _capi.make_opts(_capi.GP_F32, schedule=sched, grid_kernel=gk[args.grid_kernel],
+                           queue_tile=args.queue_tile)
     sec = C.c_double()
     stream = torch.cuda.ExternalStream(ctx.stream)
 
@@ -175,10 +180,12 @@ def run_gpu(args, rank, world, local):
                                  _capi.GP_BATCH_DEVICE_POINTERS, C.byref(sec)), "gp_ptp_batch")
         return ctx.call_stats()
 
+    plain_opts = _capi.make_opts(_capi.GP_F32)
+
     def plain():
         st = []
         for k in range(F):
-            ctx.check(L.gp_ptp_batch(ctx.handle, C.byref(dev_fields[k]), 1, C.byref(opts), _capi.GP_F32,
+            ctx.check(L.gp_ptp_batch(ctx.handle, C.byref(dev_fields[k]), 1, C.byref(plain_opts), _capi.GP_F32,
                                      _capi.GP_BATCH_DEVICE_POINTERS, C.byref(sec)), "gp_ptp_batch")
             st.append(ctx.call_stats())
         return st
@@ -268,6 +275,7 @@ def run_gpu(args, rank, world, local):
         "e2e_stats": estats[-1].as_dict(), "err": err, "e2e_equal": same, "clocks": clocks, "F": F,
         "relax_total": relax_total, "nv_total": int(voff[-1]), "meshes": meshes, "fields": fields,
         "plain_launches": sum(p.launches for p in pstats[-1]),
+        "grid_kernel": {0: "none", 1: "lockstep", 2: "queue"}.get(int(s0.grid_kernel), "?"),
     }
 
 
@@ -321,6 +329,10 @@ def main():
     ap.add_argument("--skip-check", action="store_true")
     ap.add_argument("--meshes", type=int, default=N_MESHES, help="meshes in the workload (profiling runs)")
     ap.add_argument("--only-batched", action="store_true", help="skip the plain, e2e and CPU legs (profiling runs)")
+    ap.add_argument("--schedule", default="learned", choices=["learned", "reactive"],
+                    help="batch schedule: the shipped sweep-cost model, or every field starting on one CTA")
+    ap.add_argument("--grid-kernel", default="auto", choices=["auto", "lockstep", "queue"])
+    ap.add_argument("--queue-tile", type=int, default=0, help="work-queue tile (vertices, multiple of 32)")
     args = ap.parse_args()
     rank, world, local = dist_env()
     if world > 1:
@@ -400,6 +412,7 @@ def main():
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "fields": F, "vertices_per_step": res["nv_total"] * world,
                    "relaxations_per_step": res["relax_total"] * world, "parallelism": f"fields x{world}",
+                   "schedule": args.schedule, "grid_kernel": res["grid_kernel"],
                    "l2": "inputs larger than L2 (129 MB): the step touches every mesh and field buffer"},
         "plain": {"value": plain, "unit": "fields/s", "ms_per_step": res["ms_plain"],
                   "what": "same fields, one gp_ptp_batch call per field (single-field GPU PTP)"},

@@ -41,7 +41,8 @@ class GPError(RuntimeError):
 class gp_ptp_opts(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("max_iter", C.c_uint32), ("tol", C.c_double),
                 ("threads", C.c_uint32), ("ctas", C.c_uint32), ("local_window", C.c_uint32),
-                ("round_coords", C.c_uint32), ("schedule", C.c_uint32), ("reserved", C.c_uint32)]
+                ("round_coords", C.c_uint32), ("schedule", C.c_uint32), ("grid_kernel", C.c_uint32),
+                ("queue_min", C.c_uint32), ("queue_tile", C.c_uint32)]
 
 
 class gp_ptp_stats(C.Structure):
@@ -51,7 +52,8 @@ class gp_ptp_stats(C.Structure):
 
 class gp_call_stats(C.Structure):
     _fields_ = [("launches", C.c_uint32), ("n_fields", C.c_uint32), ("fields_grid", C.c_uint32),
-                ("sweeps_grid", C.c_uint32), ("ms_toplesets", C.c_double), ("ms_renumber", C.c_double),
+                ("sweeps_grid", C.c_uint32), ("grid_kernel", C.c_uint32),
+                ("reserved", C.c_uint32), ("ms_toplesets", C.c_double), ("ms_renumber", C.c_double),
                 ("ms_local", C.c_double), ("ms_grid", C.c_double), ("ms_gather", C.c_double),
                 ("relax_local", C.c_uint64), ("relax_grid", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("d2h_bytes", C.c_uint64)]
@@ -276,10 +278,19 @@ GP_SCHED_REACTIVE = 0
 GP_SCHED_LEARNED = 1
 
 
+GP_GRID_AUTO = 0
+GP_GRID_LOCKSTEP = 1
+GP_GRID_QUEUE = 2
+
+
 def make_opts(precision: int = GP_F32, max_iter: int = 0, tol: float = 0.0, ctas: int = 0,
-              local_window: int = 0, round_coords: bool = False, schedule: int = GP_SCHED_REACTIVE) -> gp_ptp_opts:
+              local_window: int = 0, round_coords: bool = False, schedule: int = GP_SCHED_REACTIVE,
+              grid_kernel: int = GP_GRID_AUTO, queue_min: int = 0, queue_tile: int = 0) -> gp_ptp_opts:
     o = gp_ptp_opts()
+    o.queue_tile = queue_tile
     o.schedule = schedule
+    o.grid_kernel = grid_kernel
+    o.queue_min = queue_min
     o.round_coords = int(bool(round_coords))
     o.precision = precision
     o.max_iter = max_iter
@@ -313,7 +324,8 @@ def ptp(mesh: DeviceMesh, sources, limits=None, sorted_=None, dtype=np.float32, 
 
 def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP_F32, ctas: int = 0,
               with_stats: bool = True, local_window: int = 0, round_coords: bool = False,
-              schedule: int = GP_SCHED_REACTIVE):
+              schedule: int = GP_SCHED_REACTIVE, grid_kernel: int = GP_GRID_AUTO, queue_min: int = 0,
+              queue_tile: int = 0):
     """Solve many fields together (host arrays).  Returns (dists, stats, seconds)."""
     n = len(sources_list)
     out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
@@ -334,7 +346,7 @@ def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP
         fields[k].stats = C.addressof(stats[k]) if with_stats else None
     sec = C.c_double(0)
     opts = make_opts(precision, ctas=ctas, local_window=local_window, round_coords=round_coords,
-                     schedule=schedule)
+                     schedule=schedule, grid_kernel=grid_kernel, queue_min=queue_min, queue_tile=queue_tile)
     st = lib().gp_ptp_batch(ctx.handle, fields, n, C.byref(opts), out_t, 0, C.byref(sec))
     ctx.check(st, "gp_ptp_batch")
     return dists, stats, sec.value

@@ -39,7 +39,11 @@ cudaError_t launch_plan(const FieldDev *fields, const FieldState *state, uint32_
                         uint32_t local_window, uint32_t *pred_big, float *cost, uint32_t *perm, cudaStream_t s);
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
-                       cudaStream_t s);
+                       const QCtl *ctl, cudaStream_t s);
+cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fields, QField *qf, QLine *cur,
+                             QLine *done, QLine *sdone, QCtl *ctl, uint32_t ctas, uint32_t mode_req,
+                             uint32_t min_queue, uint32_t tile, bool f64, bool clusters, cudaStream_t s);
+int ptp_queue_max_ctas(int device, bool f64, bool clusters);
 uint32_t ptp_grid_max_fields();
 } // namespace gp
 
@@ -63,6 +67,7 @@ struct gp_ctx {
 	int ptp_ctas[4] = {0, 0, 0, 0};
 	int local_ctas[4] = {0, 0, 0, 0};
 	uint32_t grid_ctas = 0;    // CTAs of the last grid launch
+	int queue_ctas[4] = {};    // CTAs of the work-queue launch (all resident) per variant
 	float *model = nullptr;    // cost-model parameters (device), or null
 };
 
@@ -174,6 +179,9 @@ struct Req {
 };
 
 enum class Stage { toplesets, features, ptp };
+
+// GP_GRID_AUTO takes the work queue from this many grid fields on
+constexpr uint32_t QUEUE_MIN_DEFAULT = 0xFFFFFFFFu;
 
 struct TopOut {  // host outputs of gp_toplesets
 	uint32_t *rings;
@@ -290,6 +298,9 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_notok = cv.add<uint32_t>(3 * (size_t) F), o_bar = cv.add<uint32_t>(4);
 	const size_t o_feat = cv.add<float>((size_t) F * MLP_IN), o_pred = cv.add<float>((size_t) F * MLP_OUT);
 	const size_t o_pbig = cv.add<uint32_t>(F), o_cost = cv.add<float>(F), o_perm = cv.add<uint32_t>(F);
+	const size_t o_qf = cv.add<QField>(F), o_qcur = cv.add<QLine>((size_t) F * QUEUE_STRIPES);
+	const size_t o_qdone = cv.add<QLine>((size_t) F * QUEUE_STRIPES), o_qsd = cv.add<QLine>(F);
+	const size_t o_qctl = cv.add<QCtl>(1);
 	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
 	const size_t o_sorted = cv.add<uint32_t>(tot), o_lim = cv.add<uint32_t>(tot), o_inv = cv.add<uint32_t>(tot);
 	size_t o_cnt = 0, o_scan = 0, o_P = 0, o_Pd = 0, o_off = 0, o_fan = 0, o_D0 = 0, o_D1 = 0, o_C0 = 0, o_C1 = 0;
@@ -476,12 +487,19 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		const int maxc = ptp_max_ctas(ctx->device, f64, clusters, F);
 		uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
 		ctx->grid_ctas = ctas;
+		const uint32_t qmax = (uint32_t) ctx->queue_ctas[kv];
+		const uint32_t qctas = o.ctas ? std::min<uint32_t>(o.ctas, qmax) : qmax;
+		QCtl *dctl = reinterpret_cast<QCtl *>(P(o_qctl));
+		GP_CUDA(ctx, launch_ptp_queue(dF, dS, F, reinterpret_cast<QField *>(P(o_qf)), reinterpret_cast<QLine *>(P(o_qcur)),
+		                              reinterpret_cast<QLine *>(P(o_qdone)), reinterpret_cast<QLine *>(P(o_qsd)), dctl,
+		                              qctas, o.grid_kernel, o.queue_min ? o.queue_min : QUEUE_MIN_DEFAULT, o.queue_tile, f64,
+		                              clusters, s));
 		GP_CUDA(ctx, launch_ptp(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_notok)),
 		                        reinterpret_cast<uint32_t *>(P(o_bar)), ctas, f64, clusters, ctx->steps,
-		                        ctx->steps_cap, s));
+		                        ctx->steps_cap, dctl, s));
 		GP_CUDA(ctx, cudaEventRecord(ctx->ph[4], s));
 		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s));
-		cs.launches += 4;
+		cs.launches += 6;
 	}
 	else
 		for(int k = 2; k < 5; k++) GP_CUDA(ctx, cudaEventRecord(ctx->ph[k], s));
@@ -509,11 +527,13 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	GP_CUDA(ctx, cudaStreamSynchronize(s));
 	uint32_t ferr = 0;
 	for(uint32_t f = 0; f < F; f++) ferr |= hs[f].status;
+	QCtl hctl{};
 	if(stage == Stage::ptp)
 	{
 		uint32_t gb[4];
 		GP_CUDA(ctx, cudaMemcpy(gb, P(o_bar), sizeof(gb), cudaMemcpyDeviceToHost));
-		ferr |= gb[2];
+		GP_CUDA(ctx, cudaMemcpy(&hctl, P(o_qctl), sizeof(hctl), cudaMemcpyDeviceToHost));
+		ferr |= gb[2] | hctl.err;
 	}
 	st = map_dev_err(ctx, hsync[0].err | hsync[1].err | ferr, stage == Stage::ptp ? "ptp" : "toplesets");
 	if(st != GP_OK) return st;
@@ -540,9 +560,10 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		uint32_t hbar[4] = {0, 0, 0, 0};
 		if(stage == Stage::ptp)
 			GP_CUDA(ctx, cudaMemcpy(hbar, P(o_bar), sizeof(hbar), cudaMemcpyDeviceToHost));
-		cs.sweeps_grid = ctx->grid_ctas ? hbar[0] / ctx->grid_ctas : 0;
+		cs.grid_kernel = hctl.mode;
+		cs.sweeps_grid = hctl.mode == GRID_QUEUE ? hctl.progress : ctx->grid_ctas ? hbar[0] / ctx->grid_ctas : 0;
 		cs.h2d_bytes = h2d;
-		cs.d2h_bytes = d2h + (stage == Stage::ptp ? 2 * sizeof(hbar) : 0);
+		cs.d2h_bytes = d2h + (stage == Stage::ptp ? 2 * sizeof(hbar) + sizeof(hctl) : 0);
 		ctx->last = cs;
 	}
 	for(uint32_t f = 0; f < F; f++)
@@ -634,6 +655,7 @@ gp_status gp_ctx_create(int device, gp_ctx **out)
 	for(int k = 0; k < 4; k++)
 	{
 		ctx->ptp_ctas[k] = ptp_max_ctas(device, k >= 2, k & 1, 1);
+		ctx->queue_ctas[k] = ptp_queue_max_ctas(device, k >= 2, k & 1);
 		ctx->local_ctas[k] = ptp_local_max_ctas(device, k >= 2, k & 1);
 	}
 	for(int k = 0; k < 6; k++)

@@ -33,11 +33,35 @@ __device__ __forceinline__ uint32_t atom_add_acq_rel(uint32_t *p, uint32_t v)
 	return old;
 }
 
+__device__ __forceinline__ unsigned long long atom_add_acquire(unsigned long long *p, unsigned long long v)
+{
+	unsigned long long old;
+	asm volatile("atom.acquire.gpu.global.add.u64 %0, [%1], %2;" : "=l"(old) : "l"(p), "l"(v) : "memory");
+	return old;
+}
+
 __device__ __forceinline__ uint32_t ld_relaxed(const uint32_t *p)
 {
 	uint32_t v;
 	asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
 	return v;
+}
+
+__device__ __forceinline__ unsigned long long ld_relaxed(const unsigned long long *p)
+{
+	unsigned long long v;
+	asm volatile("ld.relaxed.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void st_relaxed(uint32_t *p, uint32_t v)
+{
+	asm volatile("st.relaxed.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long long v)
+{
+	asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
 // Grid-wide barrier of a cooperative launch.  The last CTA to arrive runs

@@ -37,6 +37,40 @@ struct GridSync {
 	uint32_t abort;  // set once any CTA gives up; the others leave at their next barrier
 };
 
+// Work-queue sweeps (ptp_queue_kernel).  Each queued field has QUEUE_STRIPES
+// claim cursors (one 128-byte line each, so claims on different stripes hit
+// different L2 lines) and as many completion counters.  A cursor packs
+// epoch (12 bits, the field's sweep number mod 4096) | tiles (26) | next tile (26).
+constexpr uint32_t QUEUE_STRIPES = 4;
+constexpr uint32_t GRID_NONE = 0, GRID_LOCKSTEP = 1, GRID_QUEUE = 2;
+
+struct alignas(128) QLine {
+	unsigned long long w;
+	uint32_t pad[30];
+};
+
+// Schedule of one queued field; only the warp that completes a sweep reads
+// and writes it (relaxed loads and stores, ordered by the completion counters).
+struct QField {
+	uint4 sched[2];      // per epoch parity: win_s, win_e, chk_e, d | groups << 1
+	uint32_t f;          // field id
+	uint32_t n_limits, max_iter, i, j, d, iter, n_iter;
+	uint32_t notok[2];   // per epoch parity: a ring-i vertex failed the test
+	uint32_t pad[2];
+	unsigned long long relax;
+};
+
+struct QCtl {
+	uint32_t G;          // fields handed to the grid-wide sweeps
+	uint32_t mode;       // GRID_NONE, GRID_LOCKSTEP or GRID_QUEUE
+	uint32_t live;       // queued fields still running
+	uint32_t progress;   // sweeps completed by the queue kernel
+	uint32_t abort;
+	uint32_t err;        // DEV_ERR_* bits
+	uint32_t warps;      // warps of the queue launch
+	uint32_t groups;     // 32-vertex groups per claimed tile; 0: chosen per window
+};
+
 // A mesh on the device, original vertex numbering.
 struct MeshDev {
 	const float4 *pos;       // nv (x, y, z, 0)

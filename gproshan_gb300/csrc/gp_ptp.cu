@@ -653,6 +653,7 @@ struct GridArgs {
 	uint32_t *bar;    // [0] arrivals (zeroed), [1] abort, [2] error bits
 	unsigned long long *steps;  // null, or 2 words per step: start time (ns), tiles << 32 | live fields
 	uint32_t steps_cap;
+	const QCtl *ctl;            // null, or the launch-mode choice (runs only if mode == GRID_LOCKSTEP)
 };
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -722,6 +723,7 @@ __global__ void __launch_bounds__(NT, 3) ptp_kernel(GridArgs a)
 	const uint32_t F = a.n_fields;
 	// compacted: entry q describes field id[q]; only fields handed to the grid.
 	// Layout: 8-byte counters first, then 4-byte-aligned arrays.
+	if(a.ctl && a.ctl->mode != GRID_LOCKSTEP) return;
 	unsigned long long *rx = reinterpret_cast<unsigned long long *>(smem);
 	SchedSmem *fs = reinterpret_cast<SchedSmem *>(rx + F);
 	uint32_t *ts = reinterpret_cast<uint32_t *>(fs + F);
@@ -849,6 +851,283 @@ size_t grid_smem_bytes(uint32_t F)
 {
 	static_assert(sizeof(SchedSmem) % 4 == 0, "layout");
 	return 8 * (size_t) F + sizeof(SchedSmem) * F + 4 * (size_t) (F + 1) + 4 * (size_t) F;
+}
+
+// ---------------------------------------------------------------------------
+// Work-queue sweeps: the grid-wide sweeps without a grid-wide barrier.
+//
+// Fields are independent; sweep s+1 of a field needs only sweep s of the same
+// field to be complete.  So every warp of one persistent launch claims tiles
+// (32 * groups consecutive window vertices) of whichever field has work,
+// relaxes them, and counts them done; the warp that completes a field's sweep
+// applies the reference's schedule rule (close_sweep / open_sweep) to that
+// field alone and publishes the next window.  A field's short sweeps no
+// longer wait for every other field's long ones, and no warp waits at a
+// barrier: tail latency of one window is filled with tiles of the others.
+//
+// Ordering: tile writes -> __syncwarp -> fence -> completion add; the warp
+// that sees the last completion fences, updates the schedule, writes the next
+// window (sched[epoch & 1]), fences and swaps the cursors.  A claim that
+// returns (epoch, k < tiles) is valid, and its sched entry cannot change until
+// that tile is counted done.  Distances are read with L2 loads (__ldcg).
+// Idle warps poll with growing sleeps and give up (error bit + abort) only if
+// no sweep of any field completes for QUEUE_IDLE_NS.
+// ---------------------------------------------------------------------------
+constexpr unsigned long long QUEUE_IDLE_NS = 2000000000ull;  // 2 s without any completed sweep
+constexpr uint32_t QB = 26;
+constexpr unsigned long long QMASK = (1ull << QB) - 1;
+constexpr uint32_t QUEUE_MAX_GROUPS = 32;  // at most 1024 vertices per tile
+
+__device__ __forceinline__ unsigned long long qpack(uint32_t epoch, uint32_t tiles)
+{
+	return ((unsigned long long) (epoch & 0xFFFu) << (2 * QB)) | ((unsigned long long) tiles << QB);
+}
+__device__ __forceinline__ uint32_t q_index(unsigned long long c) { return (uint32_t) (c & QMASK); }
+__device__ __forceinline__ uint32_t q_tiles(unsigned long long c) { return (uint32_t) ((c >> QB) & QMASK); }
+__device__ __forceinline__ uint32_t q_epoch(unsigned long long c) { return (uint32_t) (c >> (2 * QB)); }
+
+struct QueueArgs {
+	FieldDev *fields;
+	FieldState *state;
+	uint32_t n_fields;
+	QField *qf;
+	QLine *cur;    // G * QUEUE_STRIPES claim cursors
+	QLine *done;   // G * QUEUE_STRIPES completion counters
+	QLine *sdone;  // G completed-stripe counters
+	QCtl *ctl;
+};
+
+// Tile geometry of a window of nw vertices: groups of 32 vertices per tile
+// (req, or enough that a window has at most ~256 tiles: claims on one cursor
+// are serialised in L2), tiles, and non-empty stripes.
+__device__ __forceinline__ void q_geometry(uint32_t nw, uint32_t req, uint32_t &groups, uint32_t &tiles,
+                                           uint32_t &stripes)
+{
+	groups = req ? req : min(QUEUE_MAX_GROUPS, max(1u, (nw + 32u * 256u - 1) / (32u * 256u)));
+	tiles = max(1u, (nw + 32u * groups - 1) / (32u * groups));
+	stripes = min(QUEUE_STRIPES, tiles);
+}
+
+// Publish sweep `epoch` of queued field q with window [win_s, win_e).
+__device__ void q_publish(const QueueArgs &a, uint32_t q, uint32_t epoch, uint32_t win_s, uint32_t win_e,
+                          uint32_t chk_e, uint32_t d, uint32_t req)
+{
+	uint32_t groups, tiles, stripes;
+	q_geometry(win_e - win_s, req, groups, tiles, stripes);
+	QField &Q = a.qf[q];
+	Q.sched[epoch & 1u] = make_uint4(win_s, win_e, chk_e, d | (groups << 1));
+	st_relaxed(&Q.notok[epoch & 1u], 0u);
+	for(uint32_t z = 0; z < QUEUE_STRIPES; z++) st_relaxed(&a.done[q * QUEUE_STRIPES + z].w, 0ull);
+	st_relaxed(&a.sdone[q].w, 0ull);
+	__threadfence();
+	for(uint32_t z = 0; z < QUEUE_STRIPES; z++)
+	{
+		const uint32_t n = z < stripes ? (z + 1) * tiles / stripes - z * tiles / stripes : 0u;
+		atomicExch(&a.cur[q * QUEUE_STRIPES + z].w, qpack(epoch, n));
+	}
+}
+
+// The sweep `epoch` of queued field q is complete: apply the schedule rule
+// (run_ptp_gpu, src/cuda/geodesics_ptp.cu:206-229) and publish the next sweep,
+// or retire the field.  One thread.
+__device__ void q_finish(const QueueArgs &a, uint32_t q, uint32_t epoch, uint32_t req)
+{
+	QField &Q = a.qf[q];
+	const uint32_t f = Q.f;
+	const FieldDev &F = a.fields[f];
+	const uint4 sc = __ldcg(&Q.sched[epoch & 1u]);
+	FieldState st = {};
+	st.i = ld_relaxed(&Q.i);
+	st.j = ld_relaxed(&Q.j);
+	st.d = ld_relaxed(&Q.d);
+	st.iter = ld_relaxed(&Q.iter);
+	st.n_iter = ld_relaxed(&Q.n_iter);
+	st.max_iter = Q.max_iter;
+	st.n_limits = Q.n_limits;
+	st.win_s = sc.x;
+	st.win_e = sc.y;
+	st.relax = ld_relaxed(&Q.relax);
+	close_sweep(st, !ld_relaxed(&Q.notok[epoch & 1u]));
+	open_sweep(F, st, true);
+	st_relaxed(&Q.i, st.i);
+	st_relaxed(&Q.j, st.j);
+	st_relaxed(&Q.d, st.d);
+	st_relaxed(&Q.iter, st.iter);
+	st_relaxed(&Q.n_iter, st.n_iter);
+	st_relaxed(&Q.relax, st.relax);
+	if(st.live) q_publish(a, q, epoch + 1, st.win_s, st.win_e, st.chk_e, st.d, req);
+	else
+	{
+		FieldState &g = a.state[f];
+		g.i = st.i;
+		g.j = st.j;
+		g.d = st.d;
+		g.iter = st.iter;
+		g.n_iter = st.n_iter;
+		g.relax = st.relax;
+		g.live = 0;
+		__threadfence();
+		atomicSub(&a.ctl->live, 1u);
+	}
+	atomicAdd(&a.ctl->progress, 1u);
+}
+
+// Compact the fields handed to the grid, choose the launch (mode_req:
+// GRID_LOCKSTEP, GRID_QUEUE, or 0 = queue when at least min_queue fields) and
+// publish every queued field's first sweep.  One CTA of 1024 threads.
+__global__ void __launch_bounds__(1024) queue_setup_kernel(QueueArgs a, uint32_t mode_req, uint32_t min_queue,
+                                                           uint32_t warps, uint32_t groups)
+{
+	__shared__ uint32_t s_G;
+	if(threadIdx.x == 0) s_G = 0;
+	__syncthreads();
+	for(uint32_t base = 0; base < a.n_fields; base += 1024)
+	{
+		const uint32_t f = base + threadIdx.x;
+		const bool on = f < a.n_fields && a.state[f].big && a.state[f].live;
+		uint32_t tot;
+		const uint32_t ex = block_exclusive_scan<1024>(on ? 1u : 0u, &tot);
+		if(on)
+		{
+			const FieldState &g = a.state[f];
+			QField &Q = a.qf[s_G + ex];
+			Q.f = f;
+			Q.n_limits = g.n_limits;
+			Q.max_iter = g.max_iter;
+			Q.i = g.i;
+			Q.j = g.j;
+			Q.d = g.d;
+			Q.iter = g.iter;
+			Q.n_iter = g.n_iter;
+			Q.relax = g.relax;
+		}
+		__syncthreads();
+		if(threadIdx.x == 0) s_G += tot;
+		__syncthreads();
+	}
+	const uint32_t G = s_G;
+	const uint32_t mode = !G ? GRID_NONE
+	                          : mode_req == GRID_LOCKSTEP || (mode_req != GRID_QUEUE && G < min_queue) ? GRID_LOCKSTEP
+	                                                                                                   : GRID_QUEUE;
+	if(mode == GRID_QUEUE)
+		for(uint32_t q = threadIdx.x; q < G; q += 1024)
+		{
+			const FieldState &g = a.state[a.qf[q].f];
+			q_publish(a, q, 0, g.win_s, g.win_e, g.chk_e, g.d, groups);
+		}
+	if(threadIdx.x == 0)
+	{
+		a.ctl->G = G;
+		a.ctl->mode = mode;
+		a.ctl->live = mode == GRID_QUEUE ? G : 0u;
+		a.ctl->progress = 0;
+		a.ctl->abort = 0;
+		a.ctl->err = 0;
+		a.ctl->warps = warps;
+		a.ctl->groups = groups;
+	}
+}
+
+template <typename T, bool CL>
+__global__ void __launch_bounds__(NT, 3) ptp_queue_kernel(QueueArgs a)
+{
+	if(a.ctl->mode != GRID_QUEUE) return;
+	const uint32_t lane = threadIdx.x & 31;
+	const uint32_t req = a.ctl->groups;
+	const uint32_t wid = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
+	const uint32_t Z = a.ctl->G * QUEUE_STRIPES;
+	// home slot: warps spread evenly over the fields' stripes; a warp looks
+	// there first and scans onwards only when its home has no work
+	const uint32_t home = wid % Z;
+	uint32_t seen = 0xFFFFFFFFu, backoff = 32;
+	unsigned long long idle_t0 = 0;
+	for(;;)
+	{
+		// claim a tile: lanes read 32 cursors at once, lane 0 claims from the
+		// first that shows work
+		unsigned long long c = 0;
+		uint32_t z = Z;
+		for(uint32_t base = 0; base < Z && z == Z; base += 32)
+		{
+			const uint32_t zz = (home + base + lane) % Z;
+			bool avail = false;
+			if(base + lane < Z)
+			{
+				const unsigned long long cv = ld_relaxed(&a.cur[zz].w);
+				avail = q_index(cv) < q_tiles(cv);
+			}
+			unsigned m = __ballot_sync(0xffffffffu, avail);
+			while(m)
+			{
+				const int l = __ffs(m) - 1;
+				m &= m - 1;
+				const uint32_t zl = __shfl_sync(0xffffffffu, zz, l);
+				unsigned long long got = 0;
+				if(lane == 0) got = atom_add_acquire(&a.cur[zl].w, 1ull);
+				got = __shfl_sync(0xffffffffu, got, 0);
+				if(q_index(got) < q_tiles(got))
+				{
+					z = zl;
+					c = got;
+					break;
+				}
+			}
+		}
+		if(z == Z)
+		{
+			uint32_t stop = 0;
+			if(lane == 0)
+			{
+				const uint32_t p = ld_relaxed(&a.ctl->progress);
+				const unsigned long long now = global_ns();
+				if(ld_relaxed(&a.ctl->live) == 0 || ld_relaxed(&a.ctl->abort)) stop = 1;
+				else if(p != seen)
+				{
+					seen = p;
+					idle_t0 = now;
+				}
+				else if(now - idle_t0 > QUEUE_IDLE_NS)
+				{
+					atomicOr(&a.ctl->err, DEV_ERR_TIMEOUT);
+					atomicExch(&a.ctl->abort, 1u);
+					stop = 1;
+				}
+			}
+			if(__shfl_sync(0xffffffffu, stop, 0)) return;
+			__nanosleep(backoff);
+			backoff = min(backoff * 2, 2048u);
+			continue;
+		}
+		backoff = 32;
+		__syncwarp();
+		const uint32_t q = z / QUEUE_STRIPES, zs = z % QUEUE_STRIPES, e = q_epoch(c);
+		const uint4 sc = __ldcg(&a.qf[q].sched[e & 1u]);
+		const uint32_t win_s = sc.x, win_e = sc.y, chk_e = sc.z, d = sc.w & 1u;
+		uint32_t groups, tiles, stripes;
+		q_geometry(win_e - win_s, req, groups, tiles, stripes);
+		const uint32_t tile = zs * tiles / stripes + q_index(c);
+		const FieldDev &F = a.fields[a.qf[q].f];
+		int bad = 0;
+		for(uint32_t g = 0; g < groups; g++)
+		{
+			const uint32_t v = win_s + (tile * groups + g) * 32u + lane;
+			if(v < win_e) bad |= sweep_vertex<T, CL, true>(F, d, v, chk_e);
+		}
+		if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.qf[q].notok[e & 1u], 1u);
+		__syncwarp();
+		uint32_t fin = 0;
+		if(lane == 0)
+		{
+			const uint32_t old = atom_add_acq_rel(reinterpret_cast<uint32_t *>(&a.done[z].w), 1u);
+			if(old + 1 == q_tiles(c))
+			{
+				const uint32_t o2 = atom_add_acq_rel(reinterpret_cast<uint32_t *>(&a.sdone[q].w), 1u);
+				fin = o2 + 1 == stripes;
+			}
+			if(fin) q_finish(a, q, e, req);
+		}
+		__syncwarp();
+	}
 }
 
 // ---------------------------------------------------------------------------
@@ -1143,6 +1422,37 @@ int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields)
 	return nsm * per;
 }
 
+static const void *ptp_queue_ptr(bool f64, bool clusters)
+{
+	if(f64)
+		return clusters ? (const void *) ptp_queue_kernel<double, true> : (const void *) ptp_queue_kernel<double, false>;
+	return clusters ? (const void *) ptp_queue_kernel<float, true> : (const void *) ptp_queue_kernel<float, false>;
+}
+
+int ptp_queue_max_ctas(int device, bool f64, bool clusters)
+{
+	int nsm = 0, per = 0;
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, ptp_queue_ptr(f64, clusters), NT, 0);
+	return nsm * per;
+}
+
+// Queue setup (which also makes the lockstep/queue choice) and the queue
+// launch; the lockstep launch follows it and runs only if it was chosen.
+cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fields, QField *qf, QLine *cur,
+                             QLine *done, QLine *sdone, QCtl *ctl, uint32_t ctas, uint32_t mode_req,
+                             uint32_t min_queue, uint32_t tile, bool f64, bool clusters, cudaStream_t s)
+{
+	if(!n_fields) return cudaSuccess;
+	QueueArgs a{fields, state, n_fields, qf, cur, done, sdone, ctl};
+	ctas = std::max<uint32_t>(ctas, 1u);
+	queue_setup_kernel<<<1, 1024, 0, s>>>(a, mode_req, min_queue, ctas * (NT / 32), std::min(tile / 32u, QUEUE_MAX_GROUPS));
+	cudaError_t e = cudaGetLastError();
+	if(e != cudaSuccess) return e;
+	void *args[] = {&a};
+	return cudaLaunchKernel(ptp_queue_ptr(f64, clusters), dim3(ctas), dim3(NT), args, 0, s);
+}
+
 int ptp_threads() { return NT; }
 
 uint32_t ptp_grid_max_fields() { return GRID_MAX_FIELDS; }
@@ -1150,14 +1460,14 @@ uint32_t ptp_grid_max_fields() { return GRID_MAX_FIELDS; }
 // notok: 3 * n_fields words; bar: 4 words.  Both zeroed here.
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
-                       cudaStream_t s)
+                       const QCtl *ctl, cudaStream_t s)
 {
 	if(!n_fields) return cudaSuccess;
 	cudaError_t e = cudaMemsetAsync(notok, 0, 3 * sizeof(uint32_t) * n_fields, s);
 	if(e == cudaSuccess) e = cudaMemsetAsync(bar, 0, 4 * sizeof(uint32_t), s);
 	if(e == cudaSuccess && steps) e = cudaMemsetAsync(steps, 0, 16 * (size_t) steps_cap, s);
 	if(e != cudaSuccess) return e;
-	GridArgs a{fields, state, n_fields, notok, bar, steps, steps_cap};
+	GridArgs a{fields, state, n_fields, notok, bar, steps, steps_cap, ctl};
 	void *args[] = {&a};
 	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters), dim3(ctas), dim3(NT), args,
 	                                   grid_smem_bytes(n_fields), s);

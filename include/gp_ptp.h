@@ -115,8 +115,21 @@ typedef struct gp_ptp_opts {
 	uint32_t round_coords; /* GP_F64 only: 1 = solve on the float-rounded coordinates
 	                          the GP_F32 path sees (an FP64 check of an FP32 run) */
 	uint32_t schedule;     /* GP_SCHED_REACTIVE (0) or GP_SCHED_LEARNED (1): see below */
-	uint32_t reserved;
+	uint32_t grid_kernel;  /* GP_GRID_AUTO (0), GP_GRID_LOCKSTEP (1) or GP_GRID_QUEUE (2) */
+	uint32_t queue_min;    /* GP_GRID_AUTO: the work queue when at least this many fields
+	                          reach the grid-wide sweeps; 0: default */
+	uint32_t queue_tile;   /* work queue: window vertices per claimed tile (a multiple of
+	                          32, at most 1024); 0: chosen per window */
 } gp_ptp_opts;
+
+/* Grid-wide sweeps of the fields that outgrow one CTA.  LOCKSTEP: one
+ * cooperative launch, one sweep of every live field per step, a grid barrier
+ * between steps.  QUEUE: one persistent launch whose warps claim tiles of any
+ * field with work; a field's next sweep opens as soon as its own sweep is
+ * complete (no grid barrier).  Same sweeps, same results. */
+#define GP_GRID_AUTO 0u
+#define GP_GRID_LOCKSTEP 1u
+#define GP_GRID_QUEUE 2u
 
 /* Batch scheduling.  REACTIVE: every field starts on one CTA and moves to the
  * grid-wide launch when a window outgrows local_window.  LEARNED: the context's
@@ -184,7 +197,9 @@ typedef struct gp_call_stats {
 	uint32_t launches;         /* kernels this library launched in the call */
 	uint32_t n_fields;
 	uint32_t fields_grid;      /* fields swept by the grid-wide launch */
-	uint32_t sweeps_grid;      /* steps of the grid-wide launch */
+	uint32_t sweeps_grid;      /* steps of the lockstep launch, or sweeps completed by the queue launch */
+	uint32_t grid_kernel;      /* GP_GRID_LOCKSTEP, GP_GRID_QUEUE, or 0 if no field reached it */
+	uint32_t reserved;
 	double ms_toplesets;       /* BFS setup + BFS */
 	double ms_renumber;        /* ring renumbering passes */
 	double ms_local;           /* classify + one-CTA-per-field sweeps */

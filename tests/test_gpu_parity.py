@@ -208,6 +208,69 @@ def test_one_cta_and_grid_paths_agree(gpu_ctx, maker, src, precision):
     assert np.array_equal(a, b)
 
 
+@pytest.mark.parametrize("precision,clusters", [(0, False), (1, False), (0, True)])
+def test_queue_and_lockstep_grid_kernels_agree(gpu_ctx, precision, clusters):
+    """The work-queue launch (no grid barrier) and the lockstep launch sweep
+    the same windows of every field, so distances, labels and sweep counts are
+    identical; both are also checked against the fields solved alone."""
+    from gproshan_gb300 import _capi, meshgen
+    meshes = [dev_mesh(gpu_ctx, *meshgen.icosphere(5, 0.1, 3)), dev_mesh(gpu_ctx, *meshgen.height_field(200, 8)),
+              dev_mesh(gpu_ctx, *meshgen.height_field(8, 5, cols=900)), dev_mesh(gpu_ctx, *meshgen.icosphere(3, 0.1, 1))]
+    rng = np.random.default_rng(7 + precision)
+    ms, srcs = [], []
+    for k in range(23):
+        mm = meshes[k % len(meshes)]
+        ms.append(mm)
+        srcs.append(rng.choice(mm.n_vertices, size=1 + k % 3, replace=False))
+    dt = np.float64 if precision else np.float32
+    out = {}
+    for gk in (_capi.GP_GRID_LOCKSTEP, _capi.GP_GRID_QUEUE):
+        fields = (_capi.gp_field * len(ms))()
+        keep, dists, labs, stats = [], [], [], [_capi.gp_ptp_stats() for _ in ms]
+        for k, (mm, sr) in enumerate(zip(ms, srcs)):
+            sr = np.ascontiguousarray(sr, np.uint32)
+            d = np.empty(mm.n_vertices, dt)
+            lab = np.zeros(mm.n_vertices, np.uint32) if clusters else None
+            keep.append(sr)
+            dists.append(d)
+            labs.append(lab)
+            fields[k].mesh = mm.handle
+            fields[k].sources = sr.ctypes.data
+            fields[k].n_sources = len(sr)
+            fields[k].dist = d.ctypes.data
+            fields[k].clusters = None if lab is None else lab.ctypes.data
+            import ctypes
+            fields[k].stats = ctypes.addressof(stats[k])
+        opts = _capi.make_opts(precision, local_window=256, grid_kernel=gk)
+        sec = _capi.C.c_double(0)
+        gpu_ctx.check(_capi.lib().gp_ptp_batch(gpu_ctx.handle, fields, len(ms), _capi.C.byref(opts),
+                                               _capi.GP_F64 if precision else _capi.GP_F32, 0,
+                                               _capi.C.byref(sec)), "gp_ptp_batch")
+        cs = gpu_ctx.call_stats()
+        assert cs.grid_kernel == gk and cs.fields_grid >= 10
+        out[gk] = (dists, labs, [(s.n_iter, s.relaxations) for s in stats])
+    a, b = out[_capi.GP_GRID_LOCKSTEP], out[_capi.GP_GRID_QUEUE]
+    assert a[2] == b[2]
+    for k in range(len(ms)):
+        assert np.array_equal(a[0][k], b[0][k]), k
+        if clusters:
+            assert np.array_equal(a[1][k], b[1][k]), k
+    for k in range(0, len(ms), 5):
+        d, _, st = _capi.ptp(ms[k], srcs[k], dtype=dt, precision=precision)
+        assert np.array_equal(d, b[0][k]) and st.n_iter == b[2][k][0], k
+
+
+def test_queue_kernel_auto_choice(gpu_ctx):
+    """GP_GRID_AUTO takes the lockstep launch below queue_min grid fields and
+    the work queue from there on."""
+    from gproshan_gb300 import _capi, meshgen
+    m = dev_mesh(gpu_ctx, *meshgen.height_field(150, 2))
+    _capi.ptp_batch(gpu_ctx, [m], [[0]], queue_min=2)
+    assert gpu_ctx.call_stats().grid_kernel == _capi.GP_GRID_LOCKSTEP
+    _capi.ptp_batch(gpu_ctx, [m] * 5, [[0], [1], [2], [300], [5000]], queue_min=2)
+    assert gpu_ctx.call_stats().grid_kernel == _capi.GP_GRID_QUEUE
+
+
 @pytest.mark.parametrize("src", [[0, 1, 2], [64, 65, 128, 0], [5, 5, 6], [4095, 4094]])
 def test_toplesets_adjacent_and_repeated_sources(gpu_ctx, oracle_lib, src):
     """Sources next to each other (and repeated) stay in ring 0 and keep the
