@@ -78,11 +78,38 @@ __device__ __forceinline__ float rcp_a(float x)
 	return y;
 }
 
+#ifndef GP_ROTATE
+#define GP_ROTATE 1
+#endif
+#ifndef GP_BRANCHFREE
+#define GP_BRANCHFREE 1
+#endif
+
 __device__ __forceinline__ float update32(const Nb32 &a, const Nb32 &b)
 {
 	// fallback value dp[dp[1] < dp[0]]
 	const float d0 = a.t + a.l, d1 = b.t + b.l;
 	const float fb = d1 < d0 ? d1 : d0;
+#if GP_BRANCHFREE
+	// every lane evaluates the whole update and the cases are selected at the
+	// end (same values as the early-return form: no divergence inside a warp)
+	const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
+	const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+	const float cx = fmaf(a.y, b.z, -a.z * b.y);
+	const float cy = fmaf(a.z, b.x, -a.x * b.z);
+	const float cz = fmaf(a.x, b.y, -a.y * b.x);
+	const float A2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+	const float dt = b.t - a.t;
+	const float r = fmaf(-dt, dt, e2);
+	const float a1 = -fmaf(a.x, ex, fmaf(a.y, ey, a.z * ez));
+	const float a0 = fmaf(b.x, ex, fmaf(b.y, ey, b.z * ez));
+	const float q01 = fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z));
+	const float delta = fmaf(a1, dt, sqrt_a(A2 * fmaxf(r, 0.f))) * rcp_a(e2);
+	float p = fmaf(a0, delta, q01 * dt) > 0.f && fmaf(a1, delta, -a.q * dt) > 0.f ? a.t + delta : fb;
+	p = r < 0.f ? fb : p;
+	p = A2 > 0.f ? p : NAN;
+	return a.t == INFINITY || b.t == INFINITY ? fb : p;
+#else
 	if(a.t == INFINITY || b.t == INFINITY) return fb;
 	const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
 	const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
@@ -102,6 +129,7 @@ __device__ __forceinline__ float update32(const Nb32 &a, const Nb32 &b)
 	if(fmaf(a0, delta, q01 * dt) > 0.f && fmaf(a1, delta, -a.q * dt) > 0.f)
 		return a.t + delta;
 	return fb;
+#endif
 }
 
 // ---------------------------------------------------------------------------
@@ -308,7 +336,10 @@ __device__ __forceinline__ Nb32 make_nb(float4 pu, float t, float4 pv, uint32_t 
 // src/cuda/geodesics_ptp.cu:234-282).  All fan indices of a vertex of valence
 // <= FB are fetched at once, the neighbours in chunks of FC (bounded
 // registers, several loads in flight).  Returns the new (hi, lo) pair.
-constexpr uint32_t FC = 4;
+#ifndef GP_FC
+#define GP_FC 4
+#endif
+constexpr uint32_t FC = GP_FC;
 
 // (bh, bl) + x, exactly in double-float
 __device__ __forceinline__ float2 df_add(float bh, float bl, float x)
@@ -717,7 +748,10 @@ __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uin
 }
 
 template <typename T, bool CL>
-__global__ void __launch_bounds__(NT, 3) ptp_kernel(GridArgs a)
+#ifndef GP_GRID_MINB
+#define GP_GRID_MINB 3
+#endif
+__global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
 	const uint32_t F = a.n_fields;
@@ -1029,7 +1063,7 @@ __global__ void __launch_bounds__(1024) queue_setup_kernel(QueueArgs a, uint32_t
 }
 
 template <typename T, bool CL>
-__global__ void __launch_bounds__(NT, 3) ptp_queue_kernel(QueueArgs a)
+__global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_queue_kernel(QueueArgs a)
 {
 	if(a.ctl->mode != GRID_QUEUE) return;
 	const uint32_t lane = threadIdx.x & 31;
@@ -1226,6 +1260,23 @@ __global__ void fill_kernel(CatArgs c)
 					r[q] = x;
 				}
 				if(n > 8) r[7] = FAN8_OVERFLOW;
+#if GP_ROTATE
+				// FP32 distances only (labels keep the reference's triangle order):
+				// start a closed star one before its lowest-numbered neighbour, the
+				// one nearest the sources in ring order.  The two triangles around
+				// it, usually the upwind ones, come first; the downwind ones after
+				// them are then skipped by the triangle pruning in step across the
+				// warp.  The minimum over the star does not depend on the order.
+				if(sizeof(T) == 4 && !CL && n >= 3 && n <= 8 && (o0f & FAN_CLOSED))
+				{
+					uint32_t m = 0;
+					for(uint32_t q = 1; q < n; q++)
+						if(r[q] < r[m]) m = q;
+					uint32_t t[8];
+					for(uint32_t q = 0; q < 8; q++) t[q] = q < n ? r[(q + m + n - 1) % n] : r[q];
+					for(uint32_t q = 0; q < 8; q++) r[q] = t[q];
+				}
+#endif
 				if(n && (o0f & FAN_CLOSED)) r[0] |= FAN_CLOSED;
 				F.fan8[2 * (size_t) k] = make_uint4(r[0], r[1], r[2], r[3]);
 				F.fan8[2 * (size_t) k + 1] = make_uint4(r[4], r[5], r[6], r[7]);
