@@ -55,15 +55,24 @@ __device__ __forceinline__ T ld_d(const T *p)
 // ---------------------------------------------------------------------------
 struct Nb32 {
 	float x, y, z;  // X = P[u] - P[v]
-	float t;        // old distance of u
+	float t;        // old distance of u, relative to the vertex's base (rounded)
+	float te;       // rounding residual of t: t + te is the relative distance to ~1e-14 of an edge
 	float q;        // |X|^2
 	float l;        // |X|
 	uint32_t u;
 };
 
+// Knuth's TwoSum: s + e == a + b exactly.
+__device__ __forceinline__ void two_sum(float a, float b, float &s, float &e)
+{
+	s = a + b;
+	const float bb = s - a;
+	e = (a - (s - bb)) + (b - bb);
+}
+
 // sqrt and reciprocal to about 1 ulp on the SFU (PTX .approx forms).  Used on
-// edge-sized offsets only: their error is ~1e-7 of an edge length, far below
-// the solver's own rounding on the distances.
+// edge-sized offsets only; correctly rounded forms give no measurable change
+// in the results (the error budget is set by the sums below, not by these).
 __device__ __forceinline__ float sqrt_a(float x)
 {
 	float y;
@@ -78,58 +87,54 @@ __device__ __forceinline__ float rcp_a(float x)
 	return y;
 }
 
-#ifndef GP_ROTATE
-#define GP_ROTATE 1
-#endif
-#ifndef GP_BRANCHFREE
-#define GP_BRANCHFREE 1
-#endif
+// A triangle's candidate: p = t + x rounded (what the minimum is taken on),
+// with the operands kept so that the winner's value can be formed exactly:
+// (t + te) + x.  Rounding every candidate to a float and carrying that into
+// the next sweep biases the minimum low by a fraction of an ulp per update;
+// on meshes with long needle triangles (edge ratios ~20:1) the ill-conditioned
+// updates then amplify it to ~1e-4 of the distance.  Forming the winner
+// exactly keeps the FP32 path within ~2e-7 of the FP64 reference there.
+struct Cand32 {
+	float p, t, x, te;
+};
 
-__device__ __forceinline__ float update32(const Nb32 &a, const Nb32 &b)
+__device__ __forceinline__ Cand32 update32(const Nb32 &a, const Nb32 &b)
 {
 	// fallback value dp[dp[1] < dp[0]]
 	const float d0 = a.t + a.l, d1 = b.t + b.l;
-	const float fb = d1 < d0 ? d1 : d0;
-#if GP_BRANCHFREE
+	const bool fb1 = d1 < d0;
+	const float fb = fb1 ? d1 : d0;
+	const float ft = fb1 ? b.t : a.t, fx = fb1 ? b.l : a.l, fe = fb1 ? b.te : a.te;
 	// every lane evaluates the whole update and the cases are selected at the
-	// end (same values as the early-return form: no divergence inside a warp)
+	// end (no divergence inside a warp)
 	const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
 	const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
 	const float cx = fmaf(a.y, b.z, -a.z * b.y);
 	const float cy = fmaf(a.z, b.x, -a.x * b.z);
 	const float cz = fmaf(a.x, b.y, -a.y * b.x);
 	const float A2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
-	const float dt = b.t - a.t;
+	const float dt = (b.t - a.t) + (b.te - a.te);
 	const float r = fmaf(-dt, dt, e2);
-	const float a1 = -fmaf(a.x, ex, fmaf(a.y, ey, a.z * ez));
-	const float a0 = fmaf(b.x, ex, fmaf(b.y, ey, b.z * ez));
-	const float q01 = fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z));
-	const float delta = fmaf(a1, dt, sqrt_a(A2 * fmaxf(r, 0.f))) * rcp_a(e2);
-	float p = fmaf(a0, delta, q01 * dt) > 0.f && fmaf(a1, delta, -a.q * dt) > 0.f ? a.t + delta : fb;
-	p = r < 0.f ? fb : p;
-	p = A2 > 0.f ? p : NAN;
-	return a.t == INFINITY || b.t == INFINITY ? fb : p;
-#else
-	if(a.t == INFINITY || b.t == INFINITY) return fb;
-	const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
-	const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-	const float cx = fmaf(a.y, b.z, -a.z * b.y);
-	const float cy = fmaf(a.z, b.x, -a.x * b.z);
-	const float cz = fmaf(a.x, b.y, -a.y * b.x);
-	const float A2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
-	if(!(A2 > 0.f)) return NAN;
-	const float dt = b.t - a.t;
-	const float r = fmaf(-dt, dt, e2);
-	if(r < 0.f) return fb;
 	const float a1 = -fmaf(a.x, ex, fmaf(a.y, ey, a.z * ez));
 	const float a0 = fmaf(b.x, ex, fmaf(b.y, ey, b.z * ez));
 	const float q01 = fmaf(a.x, b.x, fmaf(a.y, b.y, a.z * b.z));
 	// A*sqrt(r) = sqrt(A^2 r): one root per triangle
-	const float delta = fmaf(a1, dt, sqrt_a(A2 * r)) * rcp_a(e2);
-	if(fmaf(a0, delta, q01 * dt) > 0.f && fmaf(a1, delta, -a.q * dt) > 0.f)
-		return a.t + delta;
-	return fb;
-#endif
+	const float delta = fmaf(a1, dt, sqrt_a(A2 * fmaxf(r, 0.f))) * rcp_a(e2);
+	const bool planar = fmaf(a0, delta, q01 * dt) > 0.f && fmaf(a1, delta, -a.q * dt) > 0.f && !(r < 0.f);
+	Cand32 c;
+	c.p = planar ? a.t + delta : fb;
+	c.t = planar ? a.t : ft;
+	c.x = planar ? delta : fx;
+	c.te = planar ? a.te : fe;
+	if(!(A2 > 0.f)) c.p = NAN;  // degenerate triangle: ignored
+	if(a.t == INFINITY || b.t == INFINITY)
+	{
+		c.p = fb;
+		c.t = ft;
+		c.x = fx;
+		c.te = fe;
+	}
+	return c;
 }
 
 // ---------------------------------------------------------------------------
@@ -212,17 +217,17 @@ __device__ __forceinline__ double update64(const Nb64 &A0, const Nb64 &A1)
 constexpr uint32_t FB = 8;
 
 template <bool CL, bool COH>
-__device__ __forceinline__ void take32(const Nb32 &a, const Nb32 &b, float &best, uint32_t &lab, const uint32_t *Co)
+__device__ __forceinline__ void take32(const Nb32 &a, const Nb32 &b, Cand32 &best, uint32_t &lab, const uint32_t *Co)
 {
 	// A triangle whose two neighbours are both no closer than the current best
 	// cannot improve it: the edge fallback is >= min(t0, t1), and a causal
 	// planar solution lies beyond both t0 and t1 (delta = p - t0 > 0, rounding
 	// can only matter when delta is within ~1e-6 edge of 0).  Skip the solve.
-	if(fminf(a.t, b.t) >= best) return;
-	const float p = update32(a, b);
-	if(p < best)
+	if(fminf(a.t, b.t) >= best.p) return;
+	const Cand32 c = update32(a, b);
+	if(c.p < best.p)
 	{
-		best = p;
+		best = c;
 		// GPU label rule (src/cuda/geodesics_ptp.cu:277): a = x0 (next), b = x1 (prev)
 		if(CL) lab = b.t < a.t ? ld_d<uint32_t, COH>(Co + b.u) : ld_d<uint32_t, COH>(Co + a.u);
 	}
@@ -313,18 +318,29 @@ __device__ __forceinline__ float2 ld2(const float2 *p)
 	else return *p;
 }
 
-__device__ __forceinline__ float rel_to(float2 dv, float bh, float bl)
+// (t, residual): t = (dv - base) rounded, t + residual the exact difference
+// up to the lo parts' own rounding.  The hi difference is formed exactly too
+// (TwoSum): a neighbour much nearer or farther than the base (a long edge next
+// to a short one) is not within Sterbenz range, and dropping that rounding
+// biases the FP32 solver low by ~1e-5 of the distance on anisotropic meshes.
+__device__ __forceinline__ float2 rel_to(float2 dv, float bh, float bl)
 {
-	return dv.x == INFINITY ? INFINITY : (dv.x - bh) + (dv.y - bl);
+	if(dv.x == INFINITY) return make_float2(INFINITY, 0.f);
+	float h, eh;
+	two_sum(dv.x, -bh, h, eh);
+	const float l = (dv.y - bl) + eh;
+	const float t = h + l;
+	return make_float2(t, l - (t - h));
 }
 
-__device__ __forceinline__ Nb32 make_nb(float4 pu, float t, float4 pv, uint32_t u)
+__device__ __forceinline__ Nb32 make_nb(float4 pu, float2 t, float4 pv, uint32_t u)
 {
 	Nb32 n;
 	n.x = pu.x - pv.x;
 	n.y = pu.y - pv.y;
 	n.z = pu.z - pv.z;
-	n.t = t;
+	n.t = t.x;
+	n.te = t.y;
 	n.q = fmaf(n.x, n.x, fmaf(n.y, n.y, n.z * n.z));
 	n.l = sqrt_a(n.q);
 	n.u = u;
@@ -342,13 +358,17 @@ __device__ __forceinline__ Nb32 make_nb(float4 pu, float t, float4 pv, uint32_t 
 constexpr uint32_t FC = GP_FC;
 
 // (bh, bl) + x, exactly in double-float
-__device__ __forceinline__ float2 df_add(float bh, float bl, float x)
+// The new distance base + (t + te + x), formed exactly in double-float from
+// the winning candidate's operands.
+__device__ __forceinline__ float2 df_result(float bh, float bl, const Cand32 &c)
 {
-	const float s0 = bh + x;
-	const float bb = s0 - bh;
-	const float e = (bh - (s0 - bb)) + (x - bb) + bl;
-	const float h = s0 + e;
-	return make_float2(h, e - (h - s0));
+	float s, e;
+	two_sum(c.t, c.x, s, e);
+	float h0, e0;
+	two_sum(bh, s, h0, e0);
+	e0 += (bl + c.te) + e;
+	const float h = h0 + e0;
+	return make_float2(h, e0 - (h - h0));
 }
 
 // Vertices of valence above 8: the fan from the CSR lists, one neighbour at a time.
@@ -371,7 +391,7 @@ __device__ __noinline__ float2 relax32_csr(const FieldDev &F, uint32_t v, const 
 		bl = 0.f;
 	}
 	const float old_rel = vd.x == INFINITY ? INFINITY : 0.f;
-	float best = old_rel;
+	Cand32 best = {old_rel, 0.f, 0.f, 0.f};
 	const uint32_t w0 = __ldg(fan);
 	const Nb32 first = make_nb(__ldg(F.P + w0), rel_to(ld2<COH>(Do + w0), bh, bl), pv, w0);
 	Nb32 last = first;
@@ -383,8 +403,8 @@ __device__ __noinline__ float2 relax32_csr(const FieldDev &F, uint32_t v, const 
 		last = cur;
 	}
 	if(o0f & FAN_CLOSED) take32<CL, COH>(last, first, best, lab, Co);
-	if(!(best < old_rel)) return vd;
-	return df_add(bh, bl, best);
+	if(!(best.p < old_rel)) return vd;
+	return df_result(bh, bl, best);
 }
 
 template <bool CL, bool COH>
@@ -416,7 +436,7 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 		bl = 0.f;
 	}
 	const float old_rel = vd.x == INFINITY ? INFINITY : 0.f;
-	float best = old_rel;
+	Cand32 best = {old_rel, 0.f, 0.f, 0.f};
 	Nb32 first, last;
 #pragma unroll
 	for(uint32_t c = 0; c < FB; c += FC)
@@ -441,8 +461,8 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 			}
 	}
 	if(closed) take32<CL, COH>(last, first, best, lab, Co);
-	if(!(best < old_rel)) return vd;
-	return df_add(bh, bl, best);
+	if(!(best.p < old_rel)) return vd;
+	return df_result(bh, bl, best);
 }
 
 // Relax window vertex v of field F (buffers d -> d^1) and, if v is in the
@@ -1260,14 +1280,15 @@ __global__ void fill_kernel(CatArgs c)
 					r[q] = x;
 				}
 				if(n > 8) r[7] = FAN8_OVERFLOW;
-#if GP_ROTATE
-				// FP32 distances only (labels keep the reference's triangle order):
+				// FP32 path only (the FP64 path keeps the reference's triangle order,
+				// so its labels follow the reference's tie rule bit for bit):
 				// start a closed star one before its lowest-numbered neighbour, the
 				// one nearest the sources in ring order.  The two triangles around
 				// it, usually the upwind ones, come first; the downwind ones after
 				// them are then skipped by the triangle pruning in step across the
-				// warp.  The minimum over the star does not depend on the order.
-				if(sizeof(T) == 4 && !CL && n >= 3 && n <= 8 && (o0f & FAN_CLOSED))
+				// warp.  The distances do not depend on the order except through
+				// exact ties of rounded candidates.
+				if(sizeof(T) == 4 && n >= 3 && n <= 8 && (o0f & FAN_CLOSED))
 				{
 					uint32_t m = 0;
 					for(uint32_t q = 1; q < n; q++)
@@ -1276,7 +1297,6 @@ __global__ void fill_kernel(CatArgs c)
 					for(uint32_t q = 0; q < 8; q++) t[q] = q < n ? r[(q + m + n - 1) % n] : r[q];
 					for(uint32_t q = 0; q < 8; q++) r[q] = t[q];
 				}
-#endif
 				if(n && (o0f & FAN_CLOSED)) r[0] |= FAN_CLOSED;
 				F.fan8[2 * (size_t) k] = make_uint4(r[0], r[1], r[2], r[3]);
 				F.fan8[2 * (size_t) k + 1] = make_uint4(r[4], r[5], r[6], r[7]);
