@@ -17,11 +17,23 @@ events on the library's stream.
 * e2e     -- batched through the C ABI with HOST buffers: sources copied in,
              distances copied out every step (meshes stay resident, as a
              reference `che` does between calls);
-* roofline, cpu_baseline, clocks, gpu_launches -- see the design doc.
+* roofline -- the sweep launch's algorithmic bytes (48 per relaxation) over
+             its CUDA-event time, against the measured HBM copy bandwidth;
+* cpu_baseline -- the FP64 CPU restatement on all host cores, on a bounded
+             sample of the same fields, scaled by relaxations;
+* clocks, gpu_launches -- SM clocks sampled during the timed region, and the
+             library's kernel launches inside it.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 Under torchrun each rank solves its own 256-field workload (seed offset by
 rank; weak scaling), and rank 0 prints one JSON line.
+
+``--config single|grid2048|torus|fps`` instead measures one of the other
+workloads (a single 40,962-vertex icosphere field in FP32 and FP64; one
+2048^2 height field with 4 sources; a 1M-vertex anisotropic torus, one field
+with 16 sources and 16 single-source fields batched vs plain; farthest-point
+sampling of 512 points on a 2M-vertex bump field) and prints one JSON line
+for it.
 """
 from __future__ import annotations
 
@@ -333,8 +345,13 @@ def main():
                     help="batch schedule: the shipped sweep-cost model, or every field starting on one CTA")
     ap.add_argument("--grid-kernel", default="auto", choices=["auto", "lockstep", "queue"])
     ap.add_argument("--queue-tile", type=int, default=0, help="work-queue tile (vertices, multiple of 32)")
+    ap.add_argument("--config", default="batch", choices=["batch", "single", "grid2048", "torus", "fps"])
     args = ap.parse_args()
     rank, world, local = dist_env()
+    if args.config != "batch":
+        if rank == 0:
+            emit(run_config(args))
+        return
     if world > 1:
         import torch
         import torch.distributed as dist
@@ -434,6 +451,88 @@ def main():
         "gpu_launches": launches,
     }
     emit(out)
+
+
+def run_config(args):
+    """One of the non-headline workloads; returns its JSON record."""
+    from gproshan_gb300 import _capi, build, learned, meshgen
+
+    build.build()
+    ctx = _capi.Context(0)
+    learned.install(ctx)
+
+    def relerr(a, ref):
+        fin = np.isfinite(ref) & (ref > 0)
+        return float(np.max(np.abs(a[fin].astype(np.float64) - ref[fin]) / ref[fin])) if fin.any() else 0.0
+
+    def best_of(fn, reps):
+        best = None
+        for _ in range(max(1, args.warmup)):
+            fn()
+        for _ in range(reps):
+            r = fn()
+            if best is None or r[2] < best[2]:
+                best = r + (ctx.call_stats().as_dict(),)
+        return best
+
+    rec = {"config": {"workload": args.config}, "data": "synthetic", "n_gpus": 1, "dtype": "f32"}
+    if args.config == "single":
+        xyz, tri = meshgen.icosphere(6, 0.1, 0)
+        m = _capi.DeviceMesh(ctx, xyz, tri)
+        d32, st32, s32, _ = best_of(lambda: _capi.ptp_batch(ctx, [m], [[0]]), args.steps)
+        d64, st64, s64, _ = best_of(lambda: _capi.ptp_batch(ctx, [m], [[0]], dtype=np.float64, precision=1,
+                                                               round_coords=True), max(1, args.steps // 2))
+        rec.update({"metric": "ms per field (plain single-field PTP)", "value": s32 * 1e3, "unit": "ms",
+                    "higher_is_better": False, "ms_f64": s64 * 1e3, "n_iter": st32[0].n_iter,
+                    "relaxations": st32[0].relaxations, "max_rel_err": relerr(d32[0], d64[0]),
+                    "config": {"workload": "icosphere L6 (40,962 vertices), source 0"}})
+    elif args.config == "grid2048":
+        xyz, tri = meshgen.height_field(2048, 0)
+        src = np.random.default_rng(0).choice(len(xyz), 4, replace=False).astype(np.uint32)
+        m = _capi.DeviceMesh(ctx, xyz, tri)
+        d32, st32, s32, cs = best_of(lambda: _capi.ptp_batch(ctx, [m], [src]), args.steps)
+        d64, st64, _ = _capi.ptp_batch(ctx, [m], [src], dtype=np.float64, precision=1, round_coords=True)
+        rec.update({"metric": "ms per field", "value": s32 * 1e3, "unit": "ms", "higher_is_better": False,
+                    "n_iter": st32[0].n_iter, "n_iter_f64": st64[0].n_iter, "relaxations": st32[0].relaxations,
+                    "relaxations_per_s": st32[0].relaxations / s32, "max_rel_err": relerr(d32[0], d64[0]),
+                    "phases_ms": {k: cs[k] for k in ("ms_toplesets", "ms_renumber", "ms_local", "ms_grid")},
+                    "config": {"workload": "height field 2048^2 (4,194,304 vertices), 4 seeded sources"}})
+    elif args.config == "torus":
+        xyz, tri = meshgen.torus(400, 2500, seed=0)
+        m = _capi.DeviceMesh(ctx, xyz, tri)
+        s16 = np.random.default_rng(4).choice(len(xyz), 16, replace=False).astype(np.uint32)
+        d1, st1, s1, _ = best_of(lambda: _capi.ptp_batch(ctx, [m], [s16]), args.steps)
+        d64, st64, _ = _capi.ptp_batch(ctx, [m], [s16], dtype=np.float64, precision=1, round_coords=True)
+        fs = [[int(x)] for x in s16]
+        _, _, sl, csl = best_of(lambda: _capi.ptp_batch(ctx, [m] * 16, fs, schedule=_capi.GP_SCHED_LEARNED),
+                                args.steps)
+        _, _, sr, csr = best_of(lambda: _capi.ptp_batch(ctx, [m] * 16, fs), args.steps)
+        t_plain = 0.0
+        for f in fs:
+            t_plain += _capi.ptp_batch(ctx, [m], [f])[2]
+        d16, _, _ = _capi.ptp_batch(ctx, [m] * 16, fs, schedule=_capi.GP_SCHED_LEARNED)
+        d16r, _, _ = _capi.ptp_batch(ctx, [m] * 16, fs, dtype=np.float64, precision=1, round_coords=True)
+        rec.update({"metric": "distance fields/s (16 single-source fields, learned schedule)", "value": 16 / sl,
+                    "unit": "fields/s", "higher_is_better": True, "reactive_fields_per_s": 16 / sr,
+                    "plain_fields_per_s": 16 / t_plain, "batched_over_plain": t_plain / sl,
+                    "max_rel_err_16_fields": max(relerr(a, b) for a, b in zip(d16, d16r)),
+                    "one_field_16_sources": {"ms": s1 * 1e3, "n_iter": st1[0].n_iter, "n_iter_f64": st64[0].n_iter,
+                                             "relaxations": st1[0].relaxations,
+                                             "max_rel_err": relerr(d1[0], d64[0])},
+                    "config": {"workload": "torus R=1 r=0.3, 400x2500 (1M vertices), anisotropic (edge ratio "
+                                           "up to ~20:1), 16 seeded sources"}})
+    else:
+        xyz, tri = meshgen.bump_field(1414, 0)
+        m = _capi.DeviceMesh(ctx, xyz, tri)
+        t0 = time.perf_counter()
+        smp, md, sec = _capi.fps(m, 512, seeds=(0,))
+        wall = time.perf_counter() - t0
+        rec.update({"metric": "FPS fields/s (512 sequential geodesic fields)", "value": (len(smp) - 1) / wall,
+                    "unit": "fields/s", "higher_is_better": True, "device_s": sec, "wall_s": wall,
+                    "samples": len(smp), "max_dist": md,
+                    "config": {"workload": "bump field 1414^2 (1,999,396 vertices), 64 Gaussian bumps, 5% "
+                                           "displaced vertices; farthest-point sampling from vertex 0"}})
+    return rec
 
 
 def estimate_total_relax(meshes, fields):

@@ -18,6 +18,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "libgp_ptp.so")
 
 GP_OK = 0
+GP_ERR_INVALID_ARG = 1
+GP_ERR_DEVICE_TIMEOUT = 4
+GP_ERR_CAPACITY = 8
 GP_F32 = 0
 GP_F64 = 1
 GP_BATCH_DEVICE_POINTERS = 1
@@ -103,6 +106,13 @@ SIGNATURES = {
     "gp_mlp_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p, C.c_int]),
     "gp_ctx_set_cost_model": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gp_field_features": (C.c_int, [C.c_void_p, C.POINTER(gp_field), C.c_uint32, C.c_void_p]),
+    "gp_ptp_autotune": (C.c_int, [C.c_void_p, C.POINTER(gp_field), C.c_uint32, C.c_int, C.c_uint32,
+                                  C.POINTER(gp_ptp_opts), C.c_uint32]),
+    "gp_plan_create": (C.c_int, [C.c_void_p, C.POINTER(gp_field), C.c_uint32, C.POINTER(gp_ptp_opts), C.c_int,
+                                 C.POINTER(C.c_void_p)]),
+    "gp_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "gp_plan_wait": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(gp_ptp_stats)]),
+    "gp_plan_destroy": (None, [C.c_void_p]),
     "gp_fps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64,
                          C.c_double, C.POINTER(gp_ptp_opts), _u32p, C.POINTER(C.c_double),
                          C.POINTER(C.c_double)]),
@@ -112,11 +122,14 @@ _lib = None
 _lock = threading.Lock()
 _live_meshes = weakref.WeakSet()
 _live_contexts = weakref.WeakSet()
+_live_plans = weakref.WeakSet()
 
 
 @atexit.register
 def _release_all():
-    # free device meshes, then contexts, while the CUDA runtime is still up
+    # free plans and device meshes, then contexts, while the CUDA runtime is still up
+    for p in list(_live_plans):
+        p.close()
     for m in list(_live_meshes):
         m.close()
     for c in list(_live_contexts):
@@ -434,3 +447,71 @@ def field_features(ctx: Context, meshes, sources_list):
     out = np.empty((n, MLP_IN), np.float32)
     ctx.check(lib().gp_field_features(ctx.handle, fields, n, _ptr(out)), "gp_field_features")
     return out
+
+
+# ---- autotuner and CUDA-graph plans -------------------------------------------
+
+def _fields(meshes, sources, dists):
+    """gp_field array from raw pointers (ints) or host arrays."""
+    n = len(meshes)
+    fields = (gp_field * n)()
+    keep = []
+    for k in range(n):
+        src = sources[k]
+        if isinstance(src, tuple) and len(src) == 2 and isinstance(src[0], int) and src[0] > 0xFFFFFFFF:
+            fields[k].sources, fields[k].n_sources = src  # (device pointer, count)
+        else:
+            src = _u32(src)
+            keep.append(src)
+            fields[k].sources = src.ctypes.data
+            fields[k].n_sources = len(src)
+        d = dists[k]
+        fields[k].dist = d.ctypes.data if isinstance(d, np.ndarray) else d
+        fields[k].mesh = meshes[k].handle
+    return fields, keep
+
+
+def autotune(ctx: Context, meshes, sources_list, dtype=np.float32, opts: gp_ptp_opts | None = None, reps: int = 2):
+    """Best gp_ptp_opts for this batch (host arrays); see gp_ptp_autotune."""
+    out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
+    dists = [np.empty(m.n_vertices, dtype=np.float64 if out_t == GP_F64 else np.float32) for m in meshes]
+    fields, keep = _fields(meshes, sources_list, dists)
+    o = make_opts(GP_F64 if out_t == GP_F64 else GP_F32) if opts is None else opts
+    ctx.check(lib().gp_ptp_autotune(ctx.handle, fields, len(meshes), out_t, 0, C.byref(o), reps), "gp_ptp_autotune")
+    return o
+
+
+class Plan:
+    """A batched call captured in a CUDA graph (gp_plan_*).  ``sources`` are
+    (device pointer, count) pairs and ``dists`` device pointers that stay valid
+    while the plan lives."""
+
+    def __init__(self, ctx: Context, meshes, sources, dists, opts: gp_ptp_opts | None = None, dtype=np.float32):
+        self.ctx = ctx
+        self._h = C.c_void_p()
+        out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
+        fields, _ = _fields(meshes, sources, dists)
+        o = make_opts(GP_F64 if out_t == GP_F64 else GP_F32) if opts is None else opts
+        ctx.check(lib().gp_plan_create(ctx.handle, fields, len(meshes), C.byref(o), out_t, C.byref(self._h)),
+                  "gp_plan_create")
+        self.n = len(meshes)
+        _live_plans.add(self)
+
+    def launch(self, stream: int = 0):
+        self.ctx.check(lib().gp_plan_launch(self._h, C.c_void_p(stream or None)), "gp_plan_launch")
+
+    def wait(self, stream: int = 0):
+        stats = (gp_ptp_stats * self.n)()
+        self.ctx.check(lib().gp_plan_wait(self._h, C.c_void_p(stream or None), stats), "gp_plan_wait")
+        return list(stats)
+
+    def close(self):
+        if self._h:
+            lib().gp_plan_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -78,6 +78,19 @@ struct gp_mesh {
 	void *block = nullptr;     // one device allocation holding the mesh arrays
 };
 
+// One batched call captured in a CUDA graph, with its own workspace.
+struct gp_plan {
+	gp_ctx *ctx = nullptr;
+	void *ws = nullptr;
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	uint32_t n_fields = 0;
+	FieldState *state = nullptr;  // device, per field
+	QCtl *ctl = nullptr;
+	uint32_t *bar = nullptr;
+	GridSync *sync = nullptr;
+};
+
 namespace {
 
 // kernels launched by launch_scan_u32 for n elements
@@ -205,7 +218,8 @@ gp_status map_dev_err(gp_ctx *ctx, uint32_t err, const char *where)
 }
 
 gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts, gp_dtype out_type,
-              bool src_dev, bool out_dev, Stage stage, const TopOut *top, double *seconds, float *features = nullptr)
+              bool src_dev, bool out_dev, Stage stage, const TopOut *top, double *seconds, float *features = nullptr,
+              gp_plan *plan = nullptr)
 {
 	if(!ctx) return GP_ERR_INVALID_ARG;
 	if(!F) return GP_OK;
@@ -300,7 +314,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_pbig = cv.add<uint32_t>(F), o_cost = cv.add<float>(F), o_perm = cv.add<uint32_t>(F);
 	const size_t o_qf = cv.add<QField>(F), o_qcur = cv.add<QLine>((size_t) F * QUEUE_STRIPES);
 	const size_t o_qdone = cv.add<QLine>((size_t) F * QUEUE_STRIPES), o_qsd = cv.add<QLine>(F);
-	const size_t o_qctl = cv.add<QCtl>(1);
+	const size_t o_qctl = cv.add<QCtl>(1), o_model = cv.add<float>(MLP_NPARAM);
 	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
 	const size_t o_sorted = cv.add<uint32_t>(tot), o_lim = cv.add<uint32_t>(tot), o_inv = cv.add<uint32_t>(tot);
 	size_t o_cnt = 0, o_scan = 0, o_P = 0, o_Pd = 0, o_off = 0, o_fan = 0, o_D0 = 0, o_D1 = 0, o_C0 = 0, o_C1 = 0;
@@ -327,9 +341,18 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		if(!out_dev) o_out = cv.add<char>(vtot * osz);
 	}
 	const size_t o_src = cv.add<uint32_t>(stot);
-	gp_status st = ensure_ws(ctx, cv.off);
-	if(st != GP_OK) return st;
-	char *W = static_cast<char *>(ctx->ws);
+	gp_status st = GP_OK;
+	if(plan)
+	{
+		// a plan owns its workspace: later calls on the context cannot move it
+		GP_CUDA(ctx, cudaMalloc(&plan->ws, cv.off));
+	}
+	else
+	{
+		st = ensure_ws(ctx, cv.off);
+		if(st != GP_OK) return st;
+	}
+	char *W = static_cast<char *>(plan ? plan->ws : ctx->ws);
 	auto P = [&](size_t off) { return W + off; };
 
 	// ---- host-side descriptors -------------------------------------------------
@@ -443,19 +466,32 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const uint32_t *dVbase = reinterpret_cast<const uint32_t *>(P(o_vbase));
 
 	// ---- device work ---------------------------------------------------------
-	GP_CUDA(ctx, cudaMemsetAsync(dSync, 0, 2 * sizeof(GridSync), s));
+	// (captured into the plan's graph instead of run, when planning)
+	const float *model = ctx->model;
+	if(plan && model)
+	{
+		GP_CUDA(ctx, cudaMemcpyAsync(P(o_model), model, sizeof(float) * MLP_NPARAM, cudaMemcpyDeviceToDevice, s));
+		GP_CUDA(ctx, cudaStreamSynchronize(s));
+		model = reinterpret_cast<const float *>(P(o_model));
+	}
+	const int kv = (f64 ? 2 : 0) + (clusters ? 1 : 0);
+	const int maxc = stage == Stage::ptp ? ptp_max_ctas(ctx->device, f64, clusters, F) : 0;
 	gp_call_stats cs{};
 	cs.n_fields = F;
-	GP_CUDA(ctx, cudaEventRecord(ctx->ev0, s));
-	GP_CUDA(ctx, cudaEventRecord(ctx->ph[0], s));
+	auto record = [&](cudaEvent_t ev) { return plan ? cudaSuccess : cudaEventRecord(ev, s); };
+	auto device_work = [&]() -> gp_status {
+	if(plan) GP_CUDA(ctx, cudaMemsetAsync(dS, 0, sizeof(FieldState) * F, s));
+	GP_CUDA(ctx, cudaMemsetAsync(dSync, 0, 2 * sizeof(GridSync), s));
+	GP_CUDA(ctx, record(ctx->ev0));
+	GP_CUDA(ctx, record(ctx->ph[0]));
 	if(!given_tops)
 	{
 		GP_CUDA(ctx, launch_bfs_setup(dF, dS, dVbase, F, (uint32_t) vtot, s));
 		GP_CUDA(ctx, launch_toplesets(dF, dS, F, &dSync->count, (uint32_t) ctx->bfs_ctas, s));
 		cs.launches += (vtot ? 1 : 0) + 2;
 	}
-	GP_CUDA(ctx, cudaEventRecord(ctx->ph[1], s));
-	const bool learned = stage == Stage::ptp && o.schedule == GP_SCHED_LEARNED && ctx->model;
+	GP_CUDA(ctx, record(ctx->ph[1]));
+	const bool learned = stage == Stage::ptp && o.schedule == GP_SCHED_LEARNED && model;
 	float *dfeat = reinterpret_cast<float *>(P(o_feat));
 	if(stage == Stage::features || learned)
 	{
@@ -467,8 +503,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		GP_CUDA(ctx, launch_renumber_batch(dF, dS, dBase, F, (uint32_t) tot, reinterpret_cast<uint32_t *>(P(o_cnt)),
 		                                   reinterpret_cast<uint32_t *>(P(o_scan)), f64, clusters, s));
 		cs.launches += 4 + scan_launches(tot);
-		GP_CUDA(ctx, cudaEventRecord(ctx->ph[2], s));
-		const int kv = (f64 ? 2 : 0) + (clusters ? 1 : 0);
+		GP_CUDA(ctx, record(ctx->ph[2]));
 		const uint32_t lw = o.local_window ? o.local_window : 4096u;
 		uint32_t *pbig = nullptr, *perm = nullptr;
 		if(learned)
@@ -476,15 +511,14 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			pbig = reinterpret_cast<uint32_t *>(P(o_pbig));
 			perm = reinterpret_cast<uint32_t *>(P(o_perm));
 			float *pred = reinterpret_cast<float *>(P(o_pred));
-			GP_CUDA(ctx, mlp_infer_bf16_device(ctx->model, dfeat, (int) F, pred, s));
+			GP_CUDA(ctx, mlp_infer_bf16_device(model, dfeat, (int) F, pred, s));
 			GP_CUDA(ctx, launch_plan(dF, dS, F, pred, lw, pbig, reinterpret_cast<float *>(P(o_cost)), perm, s));
 			cs.launches += 2;
 		}
 		GP_CUDA(ctx, launch_classify(dF, dS, F, lw, pbig, s));
 		GP_CUDA(ctx, launch_ptp_local(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_queue)),
 		                              (uint32_t) ctx->local_ctas[kv], lw, perm, f64, clusters, s));
-		GP_CUDA(ctx, cudaEventRecord(ctx->ph[3], s));
-		const int maxc = ptp_max_ctas(ctx->device, f64, clusters, F);
+		GP_CUDA(ctx, record(ctx->ph[3]));
 		uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
 		ctx->grid_ctas = ctas;
 		const uint32_t qmax = (uint32_t) ctx->queue_ctas[kv];
@@ -497,14 +531,39 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		GP_CUDA(ctx, launch_ptp(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_notok)),
 		                        reinterpret_cast<uint32_t *>(P(o_bar)), ctas, f64, clusters, ctx->steps,
 		                        ctx->steps_cap, dctl, s));
-		GP_CUDA(ctx, cudaEventRecord(ctx->ph[4], s));
+		GP_CUDA(ctx, record(ctx->ph[4]));
 		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s));
 		cs.launches += 6;
 	}
 	else
-		for(int k = 2; k < 5; k++) GP_CUDA(ctx, cudaEventRecord(ctx->ph[k], s));
-	GP_CUDA(ctx, cudaEventRecord(ctx->ph[5], s));
-	GP_CUDA(ctx, cudaEventRecord(ctx->ev1, s));
+		for(int k = 2; k < 5; k++) GP_CUDA(ctx, record(ctx->ph[k]));
+	GP_CUDA(ctx, record(ctx->ph[5]));
+	GP_CUDA(ctx, record(ctx->ev1));
+	return GP_OK;
+	};
+	if(plan)
+	{
+		plan->n_fields = F;
+		plan->state = dS;
+		plan->ctl = reinterpret_cast<QCtl *>(P(o_qctl));
+		plan->bar = reinterpret_cast<uint32_t *>(P(o_bar));
+		plan->sync = dSync;
+		GP_CUDA(ctx, cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+		st = device_work();
+		cudaGraph_t g = nullptr;
+		const cudaError_t e = cudaStreamEndCapture(s, &g);
+		if(st != GP_OK)
+		{
+			if(g) cudaGraphDestroy(g);
+			return st;
+		}
+		GP_CUDA(ctx, e);
+		plan->graph = g;
+		GP_CUDA(ctx, cudaGraphInstantiate(&plan->exec, g, 0));
+		return GP_OK;
+	}
+	st = device_work();
+	if(st != GP_OK) return st;
 
 	// ---- downloads -------------------------------------------------------------
 	GridSync hsync[2];
@@ -576,7 +635,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		}
 
 	if(stage == Stage::features && features)
-		GP_CUDA(ctx, cudaMemcpy(features, dfeat, sizeof(float) * F * MLP_IN, cudaMemcpyDeviceToHost));
+		GP_CUDA(ctx, cudaMemcpy(features, P(o_feat), sizeof(float) * F * MLP_IN, cudaMemcpyDeviceToHost));
 	if(stage == Stage::toplesets && top)
 	{
 		const Req &r = reqs[0];
@@ -962,6 +1021,137 @@ gp_status gp_ptp_batch(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, c
 	}
 	if(seconds) *seconds = total;
 	return GP_OK;
+}
+
+gp_status gp_ptp_autotune(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, gp_dtype dist_type,
+                          uint32_t flags, gp_ptp_opts *opts, uint32_t reps)
+{
+	if(!ctx || !opts || !n_fields || !fields) return GP_ERR_INVALID_ARG;
+	reps = std::max<uint32_t>(reps, 1);
+	auto timed = [&](const gp_ptp_opts &o, double &best) -> gp_status {
+		best = INFINITY;
+		for(uint32_t r = 0; r < reps; r++)
+		{
+			double sec = 0;
+			const gp_status st = gp_ptp_batch(ctx, fields, n_fields, &o, dist_type, flags, &sec);
+			if(st != GP_OK) return st;
+			best = std::min(best, sec);
+		}
+		return GP_OK;
+	};
+	// coordinate search: the one-CTA window first (lockstep grid), then the
+	// grid launch and its tile at that window.  Every candidate runs the same
+	// sweeps, so the results do not depend on the choice.
+	gp_ptp_opts cur = *opts, best_o = *opts;
+	double best = INFINITY, t = 0;
+	cur.grid_kernel = GP_GRID_LOCKSTEP;
+	for(uint32_t lw : {1024u, 2048u, 4096u, 8192u, 16384u})
+	{
+		cur.local_window = lw;
+		const gp_status st = timed(cur, t);
+		if(st != GP_OK) return st;
+		if(t < best)
+		{
+			best = t;
+			best_o = cur;
+		}
+	}
+	cur = best_o;
+	cur.grid_kernel = GP_GRID_QUEUE;
+	for(uint32_t tile : {64u, 128u, 256u})
+	{
+		cur.queue_tile = tile;
+		const gp_status st = timed(cur, t);
+		if(st != GP_OK) return st;
+		if(t < best)
+		{
+			best = t;
+			best_o = cur;
+		}
+	}
+	*opts = best_o;
+	return GP_OK;
+}
+
+gp_status gp_plan_create(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, const gp_ptp_opts *opts,
+                         gp_dtype dist_type, gp_plan **out)
+{
+	if(!ctx || !fields || !n_fields || !out) return GP_ERR_INVALID_ARG;
+	*out = nullptr;
+	if(n_fields > ptp_grid_max_fields())
+	{
+		set_err(ctx, "a plan holds at most %u fields", ptp_grid_max_fields());
+		return GP_ERR_CAPACITY;
+	}
+	std::vector<Req> reqs(n_fields);
+	for(uint32_t f = 0; f < n_fields; f++)
+	{
+		if(fields[f].clusters)
+		{
+			set_err(ctx, "field %u: labels are not supported by plans", f);
+			return GP_ERR_INVALID_ARG;
+		}
+		reqs[f] = Req{fields[f].mesh, fields[f].sources, fields[f].n_sources, nullptr, 0, nullptr,
+		              fields[f].dist, nullptr, nullptr};
+	}
+	gp_plan *p = new gp_plan;
+	p->ctx = ctx;
+	const gp_status st = run(ctx, reqs.data(), n_fields, opts, dist_type, true, true, Stage::ptp, nullptr, nullptr,
+	                         nullptr, p);
+	if(st != GP_OK)
+	{
+		gp_plan_destroy(p);
+		return st;
+	}
+	*out = p;
+	return GP_OK;
+}
+
+gp_status gp_plan_launch(gp_plan *plan, void *stream)
+{
+	if(!plan || !plan->exec) return GP_ERR_INVALID_ARG;
+	gp_ctx *ctx = plan->ctx;
+	GP_CUDA(ctx, cudaGraphLaunch(plan->exec, stream ? static_cast<cudaStream_t>(stream) : ctx->stream));
+	return GP_OK;
+}
+
+gp_status gp_plan_wait(gp_plan *plan, void *stream, gp_ptp_stats *stats)
+{
+	if(!plan) return GP_ERR_INVALID_ARG;
+	gp_ctx *ctx = plan->ctx;
+	cudaStream_t s = stream ? static_cast<cudaStream_t>(stream) : ctx->stream;
+	const uint32_t F = plan->n_fields;
+	std::vector<FieldState> hs(F);
+	GridSync hsync[2];
+	uint32_t hbar[4];
+	QCtl hctl{};
+	GP_CUDA(ctx, cudaMemcpyAsync(hs.data(), plan->state, sizeof(FieldState) * F, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(hsync, plan->sync, sizeof(hsync), cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(hbar, plan->bar, sizeof(hbar), cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaMemcpyAsync(&hctl, plan->ctl, sizeof(hctl), cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
+	uint32_t err = hsync[0].err | hsync[1].err | hbar[2] | hctl.err;
+	for(uint32_t f = 0; f < F; f++)
+	{
+		err |= hs[f].status;
+		if(stats)
+		{
+			stats[f].n_iter = hs[f].n_iter;
+			stats[f].n_limits = hs[f].n_limits;
+			stats[f].relaxations = hs[f].relax;
+			stats[f].seconds = 0;
+		}
+	}
+	return map_dev_err(ctx, err, "plan");
+}
+
+void gp_plan_destroy(gp_plan *plan)
+{
+	if(!plan) return;
+	if(plan->exec) cudaGraphExecDestroy(plan->exec);
+	if(plan->graph) cudaGraphDestroy(plan->graph);
+	if(plan->ws) cudaFree(plan->ws);
+	delete plan;
 }
 
 uint32_t gp_mlp_n_params(void) { return (uint32_t) MLP_NPARAM; }

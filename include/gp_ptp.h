@@ -279,6 +279,38 @@ gp_status gp_mlp_train(gp_ctx *ctx, const float *X, const float *T, uint32_t n, 
  * accumulation), else the FP32 kernels of training. */
 gp_status gp_mlp_infer(gp_ctx *ctx, const float *X, uint32_t n, const float *params, float *Y, int bf16);
 
+/*
+ * Autotuner: time the batch `fields` (as gp_ptp_batch would run it, `reps`
+ * times per candidate, best device time) over the one-CTA window widths
+ * 1024..16384 with the lockstep grid launch, then the work-queue launch with
+ * tiles of 64, 128 and 256 vertices at the best width, and write the fastest
+ * setting into opts->local_window / grid_kernel / queue_tile (the other
+ * members are kept).  The fields' outputs are written by every candidate run;
+ * all candidates give identical results.  No reference counterpart (gproshan
+ * uses fixed NT/NB launch constants, include/cuda/geodesics_ptp.cuh:7-8).
+ */
+gp_status gp_ptp_autotune(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, gp_dtype dist_type,
+                          uint32_t flags, gp_ptp_opts *opts, uint32_t reps);
+
+/*
+ * Plans: one batched call captured once in a CUDA graph and replayed.
+ * The fields' sources and dist are DEVICE pointers (as with
+ * GP_BATCH_DEVICE_POINTERS) that stay valid for the plan's life: write new
+ * source ids (same counts) into them between launches.  clusters must be
+ * null; at most 2048 fields.  The plan owns its device workspace and a copy
+ * of the context's cost model taken at creation.  gp_plan_launch enqueues the
+ * graph on `stream` (null: the context's stream) and returns; gp_plan_wait
+ * synchronises `stream`, reports device-side errors and fills per-field stats
+ * (may be null; seconds is 0).  One launch of a plan at a time.  No reference
+ * counterpart (the reference runs every call step by step from the host).
+ */
+typedef struct gp_plan gp_plan;
+gp_status gp_plan_create(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, const gp_ptp_opts *opts,
+                         gp_dtype dist_type, gp_plan **plan);
+gp_status gp_plan_launch(gp_plan *plan, void *stream);
+gp_status gp_plan_wait(gp_plan *plan, void *stream, gp_ptp_stats *stats);
+void gp_plan_destroy(gp_plan *plan);
+
 /* Install (params != null, gp_mlp_n_params() floats) or remove the cost model
  * used by GP_SCHED_LEARNED on this context. */
 gp_status gp_ctx_set_cost_model(gp_ctx *ctx, const float *params);
