@@ -64,6 +64,7 @@ struct gp_ctx {
 	unsigned long long *steps = nullptr;   // grid-launch step trace (device), if enabled
 	uint32_t steps_cap = 0;
 	int bfs_ctas = 0;
+	int bfs_wide_ctas = 0;     // CTAs of the wide-field BFS launch (all resident)
 	int ptp_ctas[4] = {0, 0, 0, 0};
 	int local_ctas[4] = {0, 0, 0, 0};
 	uint32_t grid_ctas = 0;    // CTAs of the last grid launch
@@ -196,6 +197,12 @@ enum class Stage { toplesets, features, ptp };
 // GP_GRID_AUTO takes the work queue from this many grid fields on
 constexpr uint32_t QUEUE_MIN_DEFAULT = 0xFFFFFFFFu;
 
+// Toplesets of a call with at most WIDE_MAX_FIELDS fields run every field on
+// a mesh of at least WIDE_MIN_VERTICES vertices on the whole GPU (one level
+// at a time, all CTAs); the others one CTA per field.
+constexpr uint32_t WIDE_MAX_FIELDS = 8;
+constexpr uint32_t WIDE_MIN_VERTICES = 1u << 18;
+
 struct TopOut {  // host outputs of gp_toplesets
 	uint32_t *rings;
 	uint32_t *sorted;
@@ -315,6 +322,12 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_qf = cv.add<QField>(F), o_qcur = cv.add<QLine>((size_t) F * QUEUE_STRIPES);
 	const size_t o_qdone = cv.add<QLine>((size_t) F * QUEUE_STRIPES), o_qsd = cv.add<QLine>(F);
 	const size_t o_qctl = cv.add<QCtl>(1), o_model = cv.add<float>(MLP_NPARAM);
+	std::vector<uint32_t> wide;
+	if(!given_tops && F <= WIDE_MAX_FIELDS && ctx->bfs_wide_ctas > 0)
+		for(uint32_t f = 0; f < F; f++)
+			if(reqs[f].mesh->nv >= WIDE_MIN_VERTICES) wide.push_back(f);
+	const size_t o_wide = cv.add<uint32_t>(F), o_wbar = cv.add<uint32_t>(4);
+	const size_t o_wtot = cv.add<uint32_t>((size_t) std::max(ctx->bfs_wide_ctas, 1));
 	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
 	const size_t o_sorted = cv.add<uint32_t>(tot), o_lim = cv.add<uint32_t>(tot), o_inv = cv.add<uint32_t>(tot);
 	size_t o_cnt = 0, o_scan = 0, o_P = 0, o_Pd = 0, o_off = 0, o_fan = 0, o_D0 = 0, o_D1 = 0, o_C0 = 0, o_C1 = 0;
@@ -425,6 +438,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	GP_CUDA(ctx, stage_copy(o_state, hs.data(), sizeof(FieldState) * F));
 	GP_CUDA(ctx, stage_copy(o_base, base.data(), 4 * (F + 1)));
 	GP_CUDA(ctx, stage_copy(o_vbase, vbase.data(), 4 * (F + 1)));
+	if(!wide.empty()) GP_CUDA(ctx, stage_copy(o_wide, wide.data(), 4 * wide.size()));
 	if(!src_dev)
 	{
 		std::vector<uint32_t> all(stot);
@@ -487,6 +501,13 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	if(!given_tops)
 	{
 		GP_CUDA(ctx, launch_bfs_setup(dF, dS, dVbase, F, (uint32_t) vtot, s));
+		if(!wide.empty())
+		{
+			GP_CUDA(ctx, launch_toplesets_wide(dF, dS, reinterpret_cast<const uint32_t *>(P(o_wide)),
+			                                   (uint32_t) wide.size(), reinterpret_cast<uint32_t *>(P(o_wbar)),
+			                                   reinterpret_cast<uint32_t *>(P(o_wtot)), (uint32_t) ctx->bfs_wide_ctas, s));
+			cs.launches += 1;
+		}
 		GP_CUDA(ctx, launch_toplesets(dF, dS, F, &dSync->count, (uint32_t) ctx->bfs_ctas, s));
 		cs.launches += (vtot ? 1 : 0) + 2;
 	}
@@ -593,6 +614,12 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		GP_CUDA(ctx, cudaMemcpy(gb, P(o_bar), sizeof(gb), cudaMemcpyDeviceToHost));
 		GP_CUDA(ctx, cudaMemcpy(&hctl, P(o_qctl), sizeof(hctl), cudaMemcpyDeviceToHost));
 		ferr |= gb[2] | hctl.err;
+	}
+	if(!wide.empty())
+	{
+		uint32_t wb[4];
+		GP_CUDA(ctx, cudaMemcpy(wb, P(o_wbar), sizeof(wb), cudaMemcpyDeviceToHost));
+		ferr |= wb[2];
 	}
 	st = map_dev_err(ctx, hsync[0].err | hsync[1].err | ferr, stage == Stage::ptp ? "ptp" : "toplesets");
 	if(st != GP_OK) return st;
@@ -711,6 +738,7 @@ gp_status gp_ctx_create(int device, gp_ctx **out)
 	}
 	cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
 	ctx->bfs_ctas = toplesets_max_ctas(device);
+	ctx->bfs_wide_ctas = toplesets_wide_ctas(device);
 	for(int k = 0; k < 4; k++)
 	{
 		ctx->ptp_ctas[k] = ptp_max_ctas(device, k >= 2, k & 1, 1);

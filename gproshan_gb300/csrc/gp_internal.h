@@ -169,6 +169,9 @@ cudaError_t launch_max_u32(const uint32_t *in, size_t n, uint32_t *out, cudaStre
 cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
                              uint32_t ctas, cudaStream_t s);
 int toplesets_max_ctas(int device);
+int toplesets_wide_ctas(int device);
+cudaError_t launch_toplesets_wide(FieldDev *fields, FieldState *state, const uint32_t *wide, uint32_t n_wide,
+                                  uint32_t *bar, uint32_t *cta_tot, uint32_t ctas, cudaStream_t s);
 
 // gp_ptp.cu
 int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields);

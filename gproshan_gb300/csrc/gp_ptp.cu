@@ -27,7 +27,10 @@ namespace gp {
 
 namespace {
 
-constexpr int NT = 256;  // threads of a grid-launch CTA (one tile = NT window vertices)
+#ifndef GP_NT
+#define GP_NT 256
+#endif
+constexpr int NT = GP_NT;  // threads of a grid-launch CTA
 
 // Distance/label load: coherent (L2) when other CTAs of the launch write the
 // buffer, plain otherwise.
@@ -1089,6 +1092,19 @@ __global__ void __launch_bounds__(1024) queue_setup_kernel(QueueArgs a, uint32_t
 	}
 }
 
+__device__ __forceinline__ void red_add_release(uint32_t *p, uint32_t v)
+{
+	asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// A warp holds at most one unprocessed claim besides the tile it works on:
+// while it relaxes tile k it has already claimed the next tile of the same
+// stripe (the claim's latency overlaps the work).  Completions of ordinary
+// tiles are fire-and-forget adds; the warp that claimed a stripe's last tile
+// holds no other claim, waits (bounded) until the stripe's other tiles are
+// counted, and then closes the stripe, and the sweep if it was the last
+// stripe.  Every wait is for warps that hold claims and never wait
+// themselves while holding one, so the waits end.
 template <typename T, bool CL>
 __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_queue_kernel(QueueArgs a)
 {
@@ -1102,66 +1118,71 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_queue_kernel(QueueArgs a
 	const uint32_t home = wid % Z;
 	uint32_t seen = 0xFFFFFFFFu, backoff = 32;
 	unsigned long long idle_t0 = 0;
+	uint32_t z = Z;              // slot of the claim in hand (Z: none)
+	unsigned long long c = 0;    // the claim in hand
 	for(;;)
 	{
-		// claim a tile: lanes read 32 cursors at once, lane 0 claims from the
-		// first that shows work
-		unsigned long long c = 0;
-		uint32_t z = Z;
-		for(uint32_t base = 0; base < Z && z == Z; base += 32)
-		{
-			const uint32_t zz = (home + base + lane) % Z;
-			bool avail = false;
-			if(base + lane < Z)
-			{
-				const unsigned long long cv = ld_relaxed(&a.cur[zz].w);
-				avail = q_index(cv) < q_tiles(cv);
-			}
-			unsigned m = __ballot_sync(0xffffffffu, avail);
-			while(m)
-			{
-				const int l = __ffs(m) - 1;
-				m &= m - 1;
-				const uint32_t zl = __shfl_sync(0xffffffffu, zz, l);
-				unsigned long long got = 0;
-				if(lane == 0) got = atom_add_acquire(&a.cur[zl].w, 1ull);
-				got = __shfl_sync(0xffffffffu, got, 0);
-				if(q_index(got) < q_tiles(got))
-				{
-					z = zl;
-					c = got;
-					break;
-				}
-			}
-		}
 		if(z == Z)
 		{
-			uint32_t stop = 0;
-			if(lane == 0)
+			// lanes read 32 cursors at once, lane 0 claims from the first that shows work
+			for(uint32_t base = 0; base < Z && z == Z; base += 32)
 			{
-				const uint32_t p = ld_relaxed(&a.ctl->progress);
-				const unsigned long long now = global_ns();
-				if(ld_relaxed(&a.ctl->live) == 0 || ld_relaxed(&a.ctl->abort)) stop = 1;
-				else if(p != seen)
+				const uint32_t zz = (home + base + lane) % Z;
+				bool avail = false;
+				if(base + lane < Z)
 				{
-					seen = p;
-					idle_t0 = now;
+					const unsigned long long cv = ld_relaxed(&a.cur[zz].w);
+					avail = q_index(cv) < q_tiles(cv);
 				}
-				else if(now - idle_t0 > QUEUE_IDLE_NS)
+				unsigned m = __ballot_sync(0xffffffffu, avail);
+				while(m)
 				{
-					atomicOr(&a.ctl->err, DEV_ERR_TIMEOUT);
-					atomicExch(&a.ctl->abort, 1u);
-					stop = 1;
+					const int l = __ffs(m) - 1;
+					m &= m - 1;
+					const uint32_t zl = __shfl_sync(0xffffffffu, zz, l);
+					unsigned long long got = 0;
+					if(lane == 0) got = atom_add_acquire(&a.cur[zl].w, 1ull);
+					got = __shfl_sync(0xffffffffu, got, 0);
+					if(q_index(got) < q_tiles(got))
+					{
+						z = zl;
+						c = got;
+						break;
+					}
 				}
 			}
-			if(__shfl_sync(0xffffffffu, stop, 0)) return;
-			__nanosleep(backoff);
-			backoff = min(backoff * 2, 2048u);
-			continue;
+			if(z == Z)
+			{
+				uint32_t stop = 0;
+				if(lane == 0)
+				{
+					const uint32_t p = ld_relaxed(&a.ctl->progress);
+					const unsigned long long now = global_ns();
+					if(ld_relaxed(&a.ctl->live) == 0 || ld_relaxed(&a.ctl->abort)) stop = 1;
+					else if(p != seen)
+					{
+						seen = p;
+						idle_t0 = now;
+					}
+					else if(now - idle_t0 > QUEUE_IDLE_NS)
+					{
+						atomicOr(&a.ctl->err, DEV_ERR_TIMEOUT);
+						atomicExch(&a.ctl->abort, 1u);
+						stop = 1;
+					}
+				}
+				if(__shfl_sync(0xffffffffu, stop, 0)) return;
+				__nanosleep(backoff);
+				backoff = min(backoff * 2, 2048u);
+				continue;
+			}
 		}
 		backoff = 32;
-		__syncwarp();
 		const uint32_t q = z / QUEUE_STRIPES, zs = z % QUEUE_STRIPES, e = q_epoch(c);
+		const bool last = q_index(c) + 1 == q_tiles(c);
+		unsigned long long nxt = 0;
+		if(!last && lane == 0) nxt = atom_add_acquire(&a.cur[z].w, 1ull);
+		__syncwarp();
 		const uint4 sc = __ldcg(&a.qf[q].sched[e & 1u]);
 		const uint32_t win_s = sc.x, win_e = sc.y, chk_e = sc.z, d = sc.w & 1u;
 		uint32_t groups, tiles, stripes;
@@ -1176,18 +1197,44 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_queue_kernel(QueueArgs a
 		}
 		if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.qf[q].notok[e & 1u], 1u);
 		__syncwarp();
-		uint32_t fin = 0;
+		uint32_t *done = reinterpret_cast<uint32_t *>(&a.done[z].w);
+		if(!last)
+		{
+			if(lane == 0) red_add_release(done, 1u);
+			nxt = __shfl_sync(0xffffffffu, nxt, 0);
+			if(q_index(nxt) < q_tiles(nxt)) c = nxt;
+			else z = Z;
+			continue;
+		}
+		uint32_t ok = 1;
 		if(lane == 0)
 		{
-			const uint32_t old = atom_add_acq_rel(reinterpret_cast<uint32_t *>(&a.done[z].w), 1u);
-			if(old + 1 == q_tiles(c))
+			const uint32_t want = q_tiles(c) - 1;
+			unsigned long long t0 = 0;
+			uint32_t polls = 0;
+			while(ld_acquire(done) < want)
+			{
+				if((++polls & 63u) == 0)
+				{
+					const unsigned long long now = global_ns();
+					if(!t0) t0 = now;
+					else if(now - t0 > QUEUE_IDLE_NS || ld_relaxed(&a.ctl->abort))
+					{
+						atomicOr(&a.ctl->err, DEV_ERR_TIMEOUT);
+						atomicExch(&a.ctl->abort, 1u);
+						ok = 0;
+						break;
+					}
+				}
+			}
+			if(ok)
 			{
 				const uint32_t o2 = atom_add_acq_rel(reinterpret_cast<uint32_t *>(&a.sdone[q].w), 1u);
-				fin = o2 + 1 == stripes;
+				if(o2 + 1 == stripes) q_finish(a, q, e, req);
 			}
-			if(fin) q_finish(a, q, e, req);
 		}
-		__syncwarp();
+		if(!__shfl_sync(0xffffffffu, ok, 0)) return;
+		z = Z;
 	}
 }
 

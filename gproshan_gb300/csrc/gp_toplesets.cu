@@ -208,6 +208,199 @@ __global__ void __launch_bounds__(BT) bfs_kernel(FieldDev *fields, FieldState *s
 	}
 }
 
+// ---------------------------------------------------------------------------
+// Wide fields: every CTA of one cooperative launch works on each level of one
+// field (fields taken one after another).  For a field on a large mesh with
+// many sources (farthest-point sampling: hundreds of sources on millions of
+// vertices) a level holds tens of thousands of vertices, more than one CTA
+// can turn over quickly.  A level costs two grid barriers:
+//   [barrier] count: the frontier is cut into one contiguous chunk per CTA;
+//             each CTA counts the vertices its chunk owns (key match);
+//   [barrier] emit:  each CTA adds up the counts of the CTAs before it, writes
+//             its owned vertices in frontier order, and at once discovers
+//             their neighbours for the next level (it knows their positions).
+// Discovering level L+2 while other CTAs still emit level L+1 is safe: those
+// keys carry positions past every level-L+1 key, so they never lower a key a
+// level-L+1 owner compares against, and only reach vertices not yet met.
+// ---------------------------------------------------------------------------
+constexpr int BG = 1024;  // threads of a wide-BFS CTA
+
+// Counting barrier over the whole launch (bar[0] arrivals, bar[1] abort,
+// bar[2] error bits); gives up after SPIN_LIMIT polls.
+__device__ __forceinline__ bool bfs_grid_barrier(uint32_t *bar, uint32_t target)
+{
+	__shared__ uint32_t s_ok;
+	__syncthreads();
+	if(threadIdx.x == 0)
+	{
+		s_ok = 1;
+		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+		uint32_t spins = 0;
+		while(ld_acquire(bar) < target)
+		{
+			if(++spins > SPIN_LIMIT || ld_relaxed(bar + 1))
+			{
+				atomicOr(bar + 2, DEV_ERR_TIMEOUT);
+				atomicExch(bar + 1, 1u);
+				s_ok = 0;
+				break;
+			}
+		}
+	}
+	__syncthreads();
+	return s_ok != 0;
+}
+
+__device__ __forceinline__ void load_row(const FieldDev &F, uint32_t v, uint4 &a, uint4 &b)
+{
+	a = __ldg(F.m.fan8 + 2 * (size_t) v);
+	b = __ldg(F.m.fan8 + 2 * (size_t) v + 1);
+}
+
+// Emit the vertices owned by frontier position p (key match) at sorted[o...]
+// in link order, set their ring, and discover their neighbours.
+__device__ __forceinline__ void emit_owned(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &a, const uint4 &b,
+                                           uint32_t mask, uint32_t o, uint32_t level)
+{
+	auto put = [&](uint32_t u) {
+		F.sorted[o] = u;
+		F.ring[u] = level + 1;
+		uint4 ua, ub;
+		load_row(F, u, ua, ub);
+		discover(F, o, u, ua, ub);
+		o++;
+	};
+	if(b.w == FAN8_OVERFLOW)
+	{
+		const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
+		for(uint32_t q = o0; q < o1; q++)
+		{
+			const uint32_t u = __ldg(F.m.fan + q);
+			if(ldcg(F.key + u) == (((unsigned long long) p << 20) | (q - o0)) + 1) put(u);
+		}
+		return;
+	}
+#pragma unroll
+	for(uint32_t q = 0; q < 8; q++)
+		if(mask & (1u << q)) put(slot_of(a, b, q));
+}
+
+__global__ void __launch_bounds__(BG, 1) bfs_grid_kernel(FieldDev *fields, FieldState *state, const uint32_t *wide,
+                                                      uint32_t n_wide, uint32_t *bar, uint32_t *cta_tot)
+{
+	__shared__ uint32_t s_pre, s_tot;
+	const uint32_t G = gridDim.x, b = blockIdx.x;
+	const uint32_t gt = b * BG + threadIdx.x, gn = G * BG;
+	uint32_t nbar = 0;
+	for(uint32_t w = 0; w < n_wide; w++)
+	{
+		const uint32_t f = wide[w];
+		const FieldDev &F = fields[f];
+		if(!state[f].bfs_live) continue;  // no sources, or a source out of range (uniform)
+		// level 0: the sources (ring 0) discover their neighbours
+		for(uint32_t p = gt; p < F.ns; p += gn)
+		{
+			const uint32_t v = ldcg(F.sorted + p);
+			uint4 ra, rb;
+			load_row(F, v, ra, rb);
+			discover(F, p, v, ra, rb);
+		}
+		uint32_t level = 0, s = 0, e = F.ns;
+		for(;;)
+		{
+			if(!bfs_grid_barrier(bar, G * ++nbar)) return;
+			const uint32_t n = e - s, chunk = (n + G - 1) / G;
+			const uint32_t c0 = s + min(n, b * chunk), c1 = s + min(n, (b + 1) * chunk);
+			// count this CTA's owned vertices; the first round's rows and masks stay in registers
+			uint32_t v0 = 0, m0 = 0, n0 = 0, tot = 0;
+			uint4 a0 = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY), b0 = a0;
+			for(uint32_t base = c0; base < c1; base += BG)
+			{
+				const uint32_t p = base + threadIdx.x;
+				uint32_t cnt = 0;
+				if(p < c1)
+				{
+					uint32_t v = ldcg(F.sorted + p), mask;
+					uint4 ra, rb;
+					load_row(F, v, ra, rb);
+					mask = owned(F, p, v, ra, rb, cnt);
+					if(base == c0)
+					{
+						v0 = v;
+						a0 = ra;
+						b0 = rb;
+						m0 = mask;
+						n0 = cnt;
+					}
+				}
+				uint32_t t;
+				block_exclusive_scan<BG>(cnt, &t);
+				tot += t;
+			}
+			if(threadIdx.x == 0) cta_tot[b] = tot;
+			if(!bfs_grid_barrier(bar, G * ++nbar)) return;
+			// offset of this CTA's chunk and the level's total
+			if(threadIdx.x == 0)
+			{
+				s_pre = 0;
+				s_tot = 0;
+			}
+			__syncthreads();
+			{
+				uint32_t pre = 0, all = 0;
+				for(uint32_t k = threadIdx.x; k < G; k += BG)
+				{
+					const uint32_t x = ldcg(cta_tot + k);
+					all += x;
+					if(k < b) pre += x;
+				}
+				if(pre) atomicAdd(&s_pre, pre);
+				if(all) atomicAdd(&s_tot, all);
+			}
+			__syncthreads();
+			const uint32_t grand = s_tot;
+			if(!grand) break;
+			uint32_t carry = e + s_pre;
+			for(uint32_t base = c0; base < c1; base += BG)
+			{
+				const uint32_t p = base + threadIdx.x;
+				uint32_t v = 0, mask = 0, cnt = 0;
+				uint4 ra = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY), rb = ra;
+				if(p < c1)
+				{
+					if(base == c0)
+					{
+						v = v0;
+						ra = a0;
+						rb = b0;
+						mask = m0;
+						cnt = n0;
+					}
+					else
+					{
+						v = ldcg(F.sorted + p);
+						load_row(F, v, ra, rb);
+						mask = owned(F, p, v, ra, rb, cnt);
+					}
+				}
+				uint32_t t;
+				const uint32_t ex = block_exclusive_scan<BG>(cnt, &t);
+				if(cnt) emit_owned(F, p, v, ra, rb, mask, carry + ex, level);
+				carry += t;
+			}
+			if(b == 0 && threadIdx.x == 0) F.limits[level + 2] = e + grand;
+			s = e;
+			e += grand;
+			level++;
+		}
+		if(b == 0 && threadIdx.x == 0)
+		{
+			state[f].n_limits = level + 2;
+			state[f].bfs_live = 0;
+		}
+	}
+}
+
 // Per-field setup: ring = NIL, key = max over the field's vertices.
 __global__ void bfs_clear_kernel(FieldDev *fields, const uint32_t *vbase, uint32_t n_fields, uint32_t total)
 {
@@ -272,6 +465,26 @@ int toplesets_max_ctas(int device)
 	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bfs_kernel, BT, 0);
 	return nsm * per;
+}
+
+int toplesets_wide_ctas(int device)
+{
+	int nsm = 0, per = 0;
+	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
+	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, bfs_grid_kernel, BG, 0);
+	return nsm * std::max(per, 0);
+}
+
+// wide: the fields (ids) run by the cooperative launch, n_wide of them;
+// bar: 4 words, zeroed here; cta_tot: ctas words.
+cudaError_t launch_toplesets_wide(FieldDev *fields, FieldState *state, const uint32_t *wide, uint32_t n_wide,
+                                  uint32_t *bar, uint32_t *cta_tot, uint32_t ctas, cudaStream_t s)
+{
+	if(!n_wide || !ctas) return cudaSuccess;
+	cudaError_t e = cudaMemsetAsync(bar, 0, 4 * sizeof(uint32_t), s);
+	if(e != cudaSuccess) return e;
+	void *args[] = {&fields, &state, &wide, &n_wide, &bar, &cta_tot};
+	return cudaLaunchCooperativeKernel((const void *) bfs_grid_kernel, dim3(ctas), dim3(BG), args, 0, s);
 }
 
 // queue: one word, zeroed here (the field ticket)

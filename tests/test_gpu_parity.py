@@ -275,6 +275,25 @@ def test_queue_kernel_auto_choice(gpu_ctx):
     assert gpu_ctx.call_stats().grid_kernel == _capi.GP_GRID_QUEUE
 
 
+@pytest.mark.parametrize("n_src", [1, 7, 300])
+def test_wide_toplesets_match_oracle(gpu_ctx, oracle_lib, n_src):
+    """A field on a mesh of >= 2^18 vertices in a call of few fields takes
+    the whole-GPU BFS (all CTAs on each level); its rings, sorted order and
+    limits still equal the reference's, and so do the distances."""
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.height_field(520, 11)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    src = np.random.default_rng(n_src).choice(len(xyz), n_src, replace=False)
+    r_o, s_o, l_o = oracle_lib.toplesets(om, src)
+    rings, srt, lim = _capi.toplesets(m, src)
+    assert np.array_equal(lim, l_o) and np.array_equal(srt, s_o) and np.array_equal(rings, r_o)
+    # the same field in a batch of two (both wide) and alone through gp_ptp agree
+    d2, st2, _ = _capi.ptp_batch(gpu_ctx, [m, m], [src, src[:1]])
+    d1, _, st1 = _capi.ptp(m, src)
+    assert np.array_equal(d1, d2[0]) and st1.n_iter == st2[0].n_iter and st2[0].n_limits == len(l_o)
+
+
 @pytest.mark.parametrize("src", [[0, 1, 2], [64, 65, 128, 0], [5, 5, 6], [4095, 4094]])
 def test_toplesets_adjacent_and_repeated_sources(gpu_ctx, oracle_lib, src):
     """Sources next to each other (and repeated) stay in ring 0 and keep the
