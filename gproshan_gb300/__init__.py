@@ -5,7 +5,7 @@ A drop-in for gproshan's PTP_GPU path: the same geodesics API
 ``toplesets_t``) over hand-written sm_103a CUDA in ``libgp_ptp.so``, reached
 through the C ABI declared in ``include/gp_ptp.h``.
 """
-from .che import che, NIL
+from .che import che, che_off, NIL
 from .geodesics import (
     PTP_TOL,
     farthest_point_sampling_ptp_gpu,
@@ -19,7 +19,7 @@ from .geodesics import (
 from . import _capi as capi
 
 __all__ = [
-    "che", "NIL", "PTP_TOL", "geodesics", "ptp_out_t", "toplesets_t",
+    "che", "che_off", "NIL", "PTP_TOL", "geodesics", "ptp_out_t", "toplesets_t",
     "parallel_toplesets_propagation_gpu", "parallel_toplesets_propagation_coalescence_gpu",
     "farthest_point_sampling_ptp_gpu", "normalize_ptp", "capi",
 ]

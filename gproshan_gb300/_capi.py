@@ -113,6 +113,10 @@ SIGNATURES = {
     "gp_plan_launch": (C.c_int, [C.c_void_p, C.c_void_p]),
     "gp_plan_wait": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(gp_ptp_stats)]),
     "gp_plan_destroy": (None, [C.c_void_p]),
+    "gp_off_read": (C.c_int, [C.c_char_p, _u32p, _u32p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32]),
+    "gp_mesh_create_off": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p)]),
+    "gp_che_build_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
+                                      C.POINTER(C.c_int)]),
     "gp_fps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64,
                          C.c_double, C.POINTER(gp_ptp_opts), _u32p, C.POINTER(C.c_double),
                          C.POINTER(C.c_double)]),
@@ -171,6 +175,20 @@ def che_build(n_vertices: int, tri):
     if st != GP_OK:
         raise GPError(st, "gp_che_build: triangle index out of range")
     return OT, EVT, bool(man.value)
+
+
+def off_read(path: str):
+    """(xyz, tri) of an OFF file (gp_off_read; quads split as the reference does)."""
+    nv, nf = C.c_uint32(0), C.c_uint32(0)
+    st = lib().gp_off_read(path.encode(), C.byref(nv), C.byref(nf), None, 0, None, 0)
+    if st != GP_OK:
+        raise GPError(st, f"gp_off_read({path})")
+    xyz = np.empty((nv.value, 3), np.float64)
+    tri = np.empty((nf.value, 3), np.uint32)
+    st = lib().gp_off_read(path.encode(), C.byref(nv), C.byref(nf), _ptr(xyz), nv.value, _ptr(tri), nf.value)
+    if st != GP_OK:
+        raise GPError(st, f"gp_off_read({path})")
+    return xyz, tri
 
 
 class Context:
@@ -270,6 +288,30 @@ class DeviceMesh:
             self.close()
         except Exception:
             pass
+
+
+def mesh_from_off(ctx: Context, path: str) -> DeviceMesh:
+    """gp_mesh_create_off: an OFF file to a device mesh (tables built on the GPU)."""
+    m = DeviceMesh.__new__(DeviceMesh)
+    m.ctx = ctx
+    m._h = C.c_void_p()
+    ctx.check(lib().gp_mesh_create_off(ctx.handle, path.encode(), C.byref(m._h)), "gp_mesh_create_off")
+    m.n_vertices = int(lib().gp_mesh_n_vertices(m._h))
+    m.n_faces = int(lib().gp_mesh_n_faces(m._h))
+    _live_meshes.add(m)
+    return m
+
+
+def che_build_device(ctx: Context, n_vertices: int, tri):
+    """(OT, EVT, manifold) computed on the GPU (gp_che_build_device)."""
+    VT = _u32(tri).reshape(-1)
+    nf = len(VT) // 3
+    OT = np.empty(3 * nf, np.uint32)
+    EVT = np.empty(n_vertices, np.uint32)
+    man = C.c_int(0)
+    ctx.check(lib().gp_che_build_device(ctx.handle, n_vertices, nf, _ptr(VT), _ptr(OT), _ptr(EVT), C.byref(man)),
+              "gp_che_build_device")
+    return OT, EVT, bool(man.value)
 
 
 def toplesets(mesh: DeviceMesh, sources):

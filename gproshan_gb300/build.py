@@ -20,7 +20,7 @@ LIB = os.path.join(HERE, "libgp_ptp.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
               "--expt-relaxed-constexpr"]
-SOURCES = ["gp_mesh.cu", "gp_toplesets.cu", "gp_ptp.cu", "gp_mlp.cu", "gp_capi.cpp"]
+SOURCES = ["gp_mesh.cu", "gp_toplesets.cu", "gp_ptp.cu", "gp_mlp.cu", "gp_capi.cpp", "gp_off.cpp"]
 
 
 def nvcc() -> str:

@@ -102,3 +102,14 @@ class che:
         if k != NIL:
             raise NotImplementedError("the level limit k is not used by the PTP path")
         return _capi.toplesets(self.device(ctx), sources)
+
+
+class che_off(che):
+    """A mesh read from an OFF file (che_off, include/che_off.h:11-21;
+    src/che_off.cpp:28-79): OFF/COFF/NOFF, quads split as the reference
+    splits them."""
+
+    def __init__(self, file: str):
+        xyz, tri = _capi.off_read(file)
+        super().__init__(xyz, tri)
+        self.filename = file

@@ -867,6 +867,88 @@ gp_status gp_che_build(uint32_t nv, uint32_t nf, const uint32_t *VT, uint32_t *O
 	return GP_OK;
 }
 
+gp_status gp_che_build_device(gp_ctx *ctx, uint32_t nv, uint32_t nf, const uint32_t *VT, uint32_t *OT, uint32_t *EVT,
+                              int *manifold)
+{
+	if(!ctx || (nf && (!VT || !OT)) || (nv && !EVT)) return GP_ERR_INVALID_ARG;
+	const uint64_t nhe = 3ull * nf;
+	if(nhe >= 0x7FFFFFFFull || nv >= 0x7FFFFFFFu) return GP_ERR_CAPACITY;
+	for(uint64_t he = 0; he < nhe; he++)
+		if(VT[he] >= nv)
+		{
+			set_err(ctx, "VT[%llu] out of range", (unsigned long long) he);
+			return GP_ERR_INVALID_ARG;
+		}
+	Carve c;
+	const size_t o_vt = c.add<uint32_t>(nhe), o_ot = c.add<uint32_t>(nhe), o_evt = c.add<uint32_t>(nv);
+	const size_t o_s = c.add<char>(che_build_scratch_bytes(nv, (uint32_t) nhe)), o_f = c.add<uint32_t>(4);
+	gp_status st = ensure_ws(ctx, c.off);
+	if(st != GP_OK) return st;
+	char *W = static_cast<char *>(ctx->ws);
+	cudaStream_t s = ctx->stream;
+	uint32_t f[4];
+	GP_CUDA(ctx, cudaMemcpyAsync(W + o_vt, VT, 4 * nhe, cudaMemcpyHostToDevice, s));
+	GP_CUDA(ctx, launch_che_build(reinterpret_cast<uint32_t *>(W + o_vt), nv, (uint32_t) nhe,
+	                              reinterpret_cast<uint32_t *>(W + o_ot), reinterpret_cast<uint32_t *>(W + o_evt), W + o_s,
+	                              reinterpret_cast<uint32_t *>(W + o_f), s));
+	GP_CUDA(ctx, cudaMemcpyAsync(f, W + o_f, sizeof(f), cudaMemcpyDeviceToHost, s));
+	if(nhe) GP_CUDA(ctx, cudaMemcpyAsync(OT, W + o_ot, 4 * nhe, cudaMemcpyDeviceToHost, s));
+	if(nv) GP_CUDA(ctx, cudaMemcpyAsync(EVT, W + o_evt, 4 * (size_t) nv, cudaMemcpyDeviceToHost, s));
+	GP_CUDA(ctx, cudaStreamSynchronize(s));
+	if(f[0] & 8u)
+	{
+		set_err(ctx, "an edge or border list too long for the GPU build");
+		return GP_ERR_CAPACITY;
+	}
+	if(f[0])
+	{
+		set_err(ctx, "half-edge table build: bad index (err=%u)", f[0]);
+		return GP_ERR_INVALID_ARG;
+	}
+	if(manifold) *manifold = f[1] ? 0 : 1;
+	return GP_OK;
+}
+
+gp_status gp_off_read(const char *path, uint32_t *n_vertices, uint32_t *n_faces, double *xyz, uint32_t cap_vertices,
+                      uint32_t *VT, uint32_t cap_faces)
+{
+	if(!path || !n_vertices || !n_faces) return GP_ERR_INVALID_ARG;
+	std::vector<double> X;
+	std::vector<uint32_t> T;
+	std::string err;
+	const gp_status st = off_parse(path, X, T, err);
+	if(st != GP_OK) return st;
+	*n_vertices = (uint32_t) (X.size() / 3);
+	*n_faces = (uint32_t) (T.size() / 3);
+	if(xyz)
+	{
+		if(cap_vertices < *n_vertices) return GP_ERR_CAPACITY;
+		std::memcpy(xyz, X.data(), sizeof(double) * X.size());
+	}
+	if(VT)
+	{
+		if(cap_faces < *n_faces) return GP_ERR_CAPACITY;
+		std::memcpy(VT, T.data(), sizeof(uint32_t) * T.size());
+	}
+	return GP_OK;
+}
+
+gp_status gp_mesh_create_off(gp_ctx *ctx, const char *path, gp_mesh **out)
+{
+	if(!ctx || !path || !out) return GP_ERR_INVALID_ARG;
+	std::vector<double> X;
+	std::vector<uint32_t> T;
+	std::string err;
+	const gp_status st = off_parse(path, X, T, err);
+	if(st != GP_OK)
+	{
+		set_err(ctx, "%s", err.c_str());
+		return st;
+	}
+	return gp_mesh_create(ctx, (uint32_t) (X.size() / 3), X.data(), (uint32_t) (T.size() / 3), T.data(), nullptr,
+	                      nullptr, out);
+}
+
 gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t nf, const uint32_t *VT,
                          const uint32_t *OT, const uint32_t *EVT, gp_mesh **out)
 {
@@ -879,18 +961,15 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 	}
 	const uint32_t nhe = 3 * nf;
 	std::vector<uint32_t> ot_b, evt_b;
-	if(!OT || !EVT)
+	const bool build = !OT || !EVT;  // half-edge tables built on the GPU
+	if(build)
 	{
-		ot_b.resize(nhe);
-		evt_b.resize(nv);
-		gp_status s0 = gp_che_build(nv, nf, VT, ot_b.data(), evt_b.data(), nullptr);
-		if(s0 != GP_OK)
-		{
-			set_err(ctx, "gp_che_build failed: a triangle references a vertex out of range");
-			return s0;
-		}
-		OT = ot_b.data();
-		EVT = evt_b.data();
+		for(uint32_t he = 0; he < nhe; he++)
+			if(VT[he] >= nv)
+			{
+				set_err(ctx, "VT[%u] = %u out of range (n_vertices %u)", he, VT[he], nv);
+				return GP_ERR_INVALID_ARG;
+			}
 	}
 	else
 	{
@@ -915,12 +994,40 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 	const size_t t_cnt = tc.add<uint32_t>(nv + 1), t_flags = tc.add<uint32_t>(nv);
 	const size_t t_scan = tc.add<uint32_t>(scan_tmp_words(nv)), t_xyz = tc.add<double>(3 * (size_t) nv);
 	const size_t t_err = tc.add<uint32_t>(4), t_acc = tc.add<double>(8);
+	const size_t t_che = build ? tc.add<char>(che_build_scratch_bytes(nv, nhe)) : 0, t_cf = tc.add<uint32_t>(4);
 	gp_status st = ensure_ws(ctx, tc.off);
 	if(st != GP_OK) return st;
 	char *T = static_cast<char *>(ctx->ws);
 	GP_CUDA(ctx, cudaMemcpyAsync(T + t_vt, VT, 4 * (size_t) nhe, cudaMemcpyHostToDevice, s));
-	GP_CUDA(ctx, cudaMemcpyAsync(T + t_ot, OT, 4 * (size_t) nhe, cudaMemcpyHostToDevice, s));
-	GP_CUDA(ctx, cudaMemcpyAsync(T + t_evt, EVT, 4 * (size_t) nv, cudaMemcpyHostToDevice, s));
+	if(build)
+	{
+		uint32_t cf[4];
+		GP_CUDA(ctx, launch_che_build(reinterpret_cast<uint32_t *>(T + t_vt), nv, nhe, reinterpret_cast<uint32_t *>(T + t_ot),
+		                              reinterpret_cast<uint32_t *>(T + t_evt), T + t_che,
+		                              reinterpret_cast<uint32_t *>(T + t_cf), s));
+		GP_CUDA(ctx, cudaMemcpyAsync(cf, T + t_cf, sizeof(cf), cudaMemcpyDeviceToHost, s));
+		GP_CUDA(ctx, cudaStreamSynchronize(s));
+		if(cf[0] & ~8u)
+		{
+			set_err(ctx, "half-edge table build: bad index (err=%u)", cf[0]);
+			return GP_ERR_INVALID_ARG;
+		}
+		if(cf[0] & 8u)
+		{
+			// an edge shared by more than 32 half-edges, or a vertex with more
+			// than 32 border half-edges: the host builds the tables
+			ot_b.resize(nhe);
+			evt_b.resize(nv);
+			gp_che_build(nv, nf, VT, ot_b.data(), evt_b.data(), nullptr);
+			GP_CUDA(ctx, cudaMemcpyAsync(T + t_ot, ot_b.data(), 4 * (size_t) nhe, cudaMemcpyHostToDevice, s));
+			GP_CUDA(ctx, cudaMemcpyAsync(T + t_evt, evt_b.data(), 4 * (size_t) nv, cudaMemcpyHostToDevice, s));
+		}
+	}
+	else
+	{
+		GP_CUDA(ctx, cudaMemcpyAsync(T + t_ot, OT, 4 * (size_t) nhe, cudaMemcpyHostToDevice, s));
+		GP_CUDA(ctx, cudaMemcpyAsync(T + t_evt, EVT, 4 * (size_t) nv, cudaMemcpyHostToDevice, s));
+	}
 	GP_CUDA(ctx, cudaMemcpyAsync(T + t_xyz, xyz, 24 * (size_t) nv, cudaMemcpyHostToDevice, s));
 	GP_CUDA(ctx, cudaMemsetAsync(T + t_err, 0, 16, s));
 	uint32_t *dvt = reinterpret_cast<uint32_t *>(T + t_vt), *dot = reinterpret_cast<uint32_t *>(T + t_ot);

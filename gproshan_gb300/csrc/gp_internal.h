@@ -4,6 +4,8 @@
 #include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
+#include <string>
+#include <vector>
 
 #include "../../include/gp_ptp.h"
 
@@ -169,6 +171,10 @@ cudaError_t launch_max_u32(const uint32_t *in, size_t n, uint32_t *out, cudaStre
 cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
                              uint32_t ctas, cudaStream_t s);
 int toplesets_max_ctas(int device);
+size_t che_build_scratch_bytes(uint32_t nv, uint32_t nhe);
+gp_status off_parse(const char *path, std::vector<double> &xyz, std::vector<uint32_t> &tri, std::string &err);
+cudaError_t launch_che_build(const uint32_t *VT, uint32_t nv, uint32_t nhe, uint32_t *OT, uint32_t *EVT,
+                             void *scratch, uint32_t *flags, cudaStream_t s);
 int toplesets_wide_ctas(int device);
 cudaError_t launch_toplesets_wide(FieldDev *fields, FieldState *state, const uint32_t *wide, uint32_t n_wide,
                                   uint32_t *bar, uint32_t *cta_tot, uint32_t ctas, cudaStream_t s);

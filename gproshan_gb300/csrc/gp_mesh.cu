@@ -221,7 +221,198 @@ __global__ void scan_tile_kernel(const uint32_t *__restrict__ in, uint32_t *__re
 	if(write_total && blockIdx.x == gridDim.x - 1 && threadIdx.x == SCAN_NT - 1) out[n] = run;
 }
 
+// ---------------------------------------------------------------------------
+// Half-edge tables on the GPU: che::update_evt_ot_et (src/che.cpp:1295-1362)
+// in parallel, with its exact results, non-manifold cases included.
+//
+// The reference pairs half-edges greedily in half-edge order: an unpaired he
+// (a -> b) takes the first still-free t (b -> a) in the order of next(t).  Its
+// choices for one undirected edge {a, b} only involve the half-edges lying on
+// that edge, so the greedy splits into independent groups: the half-edges are
+// grouped by edge in a hash table, each group's smallest member runs the
+// greedy on its group (the usual group of one or two is settled at once), and
+// each vertex replays the border rule for EVT over its own border half-edges
+// in half-edge order.  A group or border list longer than CHE_LOCAL entries
+// sets a flag (the host then builds the tables instead).
+// ---------------------------------------------------------------------------
+constexpr uint32_t CHE_LOCAL = 32;
+constexpr unsigned long long CHE_EMPTY = ~0ull;
+
+__device__ __forceinline__ uint32_t che_hash(unsigned long long k, uint32_t mask)
+{
+	k ^= k >> 33;
+	k *= 0xff51afd7ed558ccdull;
+	k ^= k >> 33;
+	return (uint32_t) k & mask;
+}
+
+// EVT (last half-edge of each vertex, +1), the edge groups, per-vertex lists
+__global__ void che_group_kernel(const uint32_t *__restrict__ VT, uint32_t nhe, uint32_t nv,
+                                 unsigned long long *keys, uint32_t *heads, uint32_t mask, uint32_t *grp,
+                                 uint32_t *nextg, uint32_t *evt1, uint32_t *err)
+{
+	const uint32_t he = blockIdx.x * blockDim.x + threadIdx.x;
+	if(he >= nhe) return;
+	const uint32_t a = VT[he], b = VT[he_next(he)];
+	if(a >= nv || b >= nv)
+	{
+		atomicOr(err, DEV_ERR_BOUNDS);
+		return;
+	}
+	atomicMax(evt1 + a, he + 1);
+	const unsigned long long key = ((unsigned long long) min(a, b) << 32) | max(a, b);
+	uint32_t slot = che_hash(key, mask);
+	for(uint32_t probe = 0; probe <= mask; probe++)
+	{
+		const unsigned long long prev = atomicCAS(keys + slot, CHE_EMPTY, key);
+		if(prev == CHE_EMPTY || prev == key)
+		{
+			grp[he] = slot;
+			nextg[he] = atomicExch(heads + slot, he);
+			return;
+		}
+		slot = (slot + 1) & mask;
+	}
+	atomicOr(err, DEV_ERR_BOUNDS);  // table full: cannot happen at 2x load
+}
+
+__device__ __forceinline__ void sort_small(uint32_t *x, uint32_t n)
+{
+	for(uint32_t i = 1; i < n; i++)
+	{
+		const uint32_t v = x[i];
+		uint32_t j = i;
+		for(; j && x[j - 1] > v; j--) x[j] = x[j - 1];
+		x[j] = v;
+	}
+}
+
+__global__ void che_pair_kernel(const uint32_t *__restrict__ VT, uint32_t nhe, const uint32_t *heads,
+                                const uint32_t *grp, const uint32_t *nextg, uint32_t *OT, uint32_t *err)
+{
+	const uint32_t he = blockIdx.x * blockDim.x + threadIdx.x;
+	if(he >= nhe) return;
+	// the group's smallest member does the group's work
+	uint32_t m[CHE_LOCAL], n = 0, lo = he;
+	bool over = false;
+	for(uint32_t x = heads[grp[he]]; x != NIL; x = nextg[x])
+	{
+		lo = min(lo, x);
+		if(n < CHE_LOCAL) m[n++] = x;
+		else over = true;
+	}
+	if(lo != he) return;
+	if(over)
+	{
+		atomicOr(err, 8u);
+		return;
+	}
+	sort_small(m, n);
+	for(uint32_t k = 0; k < n; k++) OT[m[k]] = NIL;
+	for(uint32_t k = 0; k < n; k++)
+	{
+		const uint32_t x = m[k];
+		if(OT[x] != NIL) continue;
+		const uint32_t a = VT[x], b = VT[he_next(x)];
+		// candidates t (b -> a) of the group, in the order of next(t)
+		uint32_t cand[CHE_LOCAL], nc = 0;
+		for(uint32_t q = 0; q < n; q++)
+		{
+			const uint32_t t = m[q];
+			if(VT[t] == b && VT[he_next(t)] == a) cand[nc++] = he_next(t);
+		}
+		sort_small(cand, nc);
+		for(uint32_t q = 0; q < nc; q++)
+		{
+			const uint32_t t = he_prev(cand[q]);
+			if(OT[x] == NIL && OT[t] == NIL)
+			{
+				OT[x] = t;
+				OT[t] = x;
+			}
+		}
+	}
+}
+
+// border half-edges listed per vertex
+__global__ void che_border_kernel(const uint32_t *__restrict__ VT, const uint32_t *__restrict__ OT, uint32_t nhe,
+                                  uint32_t *bhead, uint32_t *bnext)
+{
+	const uint32_t he = blockIdx.x * blockDim.x + threadIdx.x;
+	if(he >= nhe || OT[he] != NIL) return;
+	bnext[he] = atomicExch(bhead + VT[he], he);
+}
+
+// EVT: the last half-edge of the vertex, then the border rule replayed over
+// the vertex's border half-edges in order; flags[1] = 1 if non-manifold
+__global__ void che_evt_kernel(const uint32_t *__restrict__ OT, uint32_t nv, const uint32_t *evt1,
+                               const uint32_t *bhead, const uint32_t *bnext, uint32_t *EVT, uint32_t *err,
+                               uint32_t *nonmanifold)
+{
+	const uint32_t v = blockIdx.x * blockDim.x + threadIdx.x;
+	if(v >= nv) return;
+	uint32_t e = evt1[v] - 1u;  // NIL when the vertex has no half-edge
+	uint32_t b[CHE_LOCAL], n = 0;
+	for(uint32_t x = bhead[v]; x != NIL; x = bnext[x])
+	{
+		if(n == CHE_LOCAL)
+		{
+			atomicOr(err, 8u);
+			return;
+		}
+		b[n++] = x;
+	}
+	sort_small(b, n);
+	for(uint32_t k = 0; k < n; k++)
+	{
+		if(e == NIL) continue;
+		if(OT[e] == NIL && e != b[k])
+		{
+			e = NIL;
+			atomicExch(nonmanifold, 1u);
+		}
+		else e = b[k];
+	}
+	EVT[v] = e;
+}
+
 } // namespace
+
+size_t che_build_scratch_bytes(uint32_t nv, uint32_t nhe)
+{
+	uint32_t T = 1;
+	while(T < 2 * std::max(nhe, 1u)) T <<= 1;
+	return 8ull * T + 4ull * T + 4ull * nhe * 3 + 4ull * nv * 2 + 4096;
+}
+
+// VT (device) -> OT, EVT (device).  flags: 4 words, [0] error bits (8: a
+// group or border list too long for the GPU build), [1] non-manifold.
+cudaError_t launch_che_build(const uint32_t *VT, uint32_t nv, uint32_t nhe, uint32_t *OT, uint32_t *EVT,
+                             void *scratch, uint32_t *flags, cudaStream_t s)
+{
+	uint32_t T = 1;
+	while(T < 2 * std::max(nhe, 1u)) T <<= 1;
+	char *p = static_cast<char *>(scratch);
+	unsigned long long *keys = reinterpret_cast<unsigned long long *>(p);
+	uint32_t *heads = reinterpret_cast<uint32_t *>(keys + T);
+	uint32_t *grp = heads + T, *nextg = grp + nhe, *bnext = nextg + nhe;
+	uint32_t *evt1 = bnext + nhe, *bhead = evt1 + nv;
+	cudaError_t e = cudaMemsetAsync(keys, 0xFF, 8ull * T, s);
+	if(e == cudaSuccess) e = cudaMemsetAsync(heads, 0xFF, 4ull * T, s);
+	if(e == cudaSuccess) e = cudaMemsetAsync(evt1, 0, 4ull * nv, s);
+	if(e == cudaSuccess) e = cudaMemsetAsync(bhead, 0xFF, 4ull * nv, s);
+	if(e == cudaSuccess) e = cudaMemsetAsync(flags, 0, 16, s);
+	if(e != cudaSuccess) return e;
+	const unsigned gh = (nhe + 255) / 256, gv = (nv + 255) / 256;
+	if(nhe)
+	{
+		che_group_kernel<<<gh, 256, 0, s>>>(VT, nhe, nv, keys, heads, T - 1, grp, nextg, evt1, flags);
+		che_pair_kernel<<<gh, 256, 0, s>>>(VT, nhe, heads, grp, nextg, OT, flags);
+		che_border_kernel<<<gh, 256, 0, s>>>(VT, OT, nhe, bhead, bnext);
+	}
+	if(nv) che_evt_kernel<<<gv, 256, 0, s>>>(OT, nv, evt1, bhead, bnext, EVT, flags, flags + 1);
+	return cudaGetLastError();
+}
 
 size_t scan_tmp_words(size_t n)
 {

@@ -319,6 +319,27 @@ gp_status gp_ctx_set_cost_model(gp_ctx *ctx, const float *params);
  * clusters and stats members are not used. */
 gp_status gp_field_features(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields, float *features);
 
+/*
+ * OFF input (che_off::read_file, src/che_off.cpp:28-79): OFF, COFF and NOFF
+ * files, triangles and quads (a quad a b c d becomes (a, b, c) and (d, a, c)
+ * as in the reference), '#' comments skipped.  The counts are always
+ * written; xyz (3 doubles per vertex) and VT (3 indices per triangle) are
+ * filled when not null and large enough (else GP_ERR_CAPACITY), so a first
+ * call with null arrays gives the sizes.  Host only, no device needed.
+ */
+gp_status gp_off_read(const char *path, uint32_t *n_vertices, uint32_t *n_faces, double *xyz, uint32_t cap_vertices,
+                      uint32_t *VT, uint32_t cap_faces);
+/* An OFF file straight to a device mesh: read, upload, half-edge tables
+ * built on the GPU (che::init(file), src/che.cpp:1266-1273). */
+gp_status gp_mesh_create_off(gp_ctx *ctx, const char *path, gp_mesh **mesh);
+/* The half-edge tables of gp_che_build computed on the GPU (host arrays in
+ * and out; the same OT, EVT and manifold flag, non-manifold rules included).
+ * GP_ERR_CAPACITY if an edge is shared by more than 32 half-edges or a vertex
+ * has more than 32 border half-edges (gp_mesh_create then builds on the
+ * host).  gp_mesh_create uses this build whenever OT/EVT are not given. */
+gp_status gp_che_build_device(gp_ctx *ctx, uint32_t n_vertices, uint32_t n_faces, const uint32_t *VT, uint32_t *OT,
+                              uint32_t *EVT, int *manifold);
+
 /* normalize_ptp (src/geodesics_ptp.cpp:264-276) on a host array. */
 gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n);
 

@@ -233,6 +233,29 @@ class RefLib:
         self.upd.argtypes = [C.c_void_p, rp, C.c_uint]
         self.norm = getattr(L, p + "normalize_ptp")
         self.norm.argtypes = [rp, C.c_ulonglong]
+        self.off_open = getattr(L, p + "off_open")
+        self.off_open.restype = C.c_void_p
+        self.off_open.argtypes = [C.c_char_p]
+        self.nv = getattr(L, p + "che_n_vertices")
+        self.nv.restype = C.c_uint
+        self.nv.argtypes = [C.c_void_p]
+        self.xyz = getattr(L, p + "che_xyz")
+        self.xyz.argtypes = [C.c_void_p, _f64p]
+
+    def read_off(self, path: str):
+        """(xyz, VT, OT, EVT) of an OFF file read by the reference's che_off."""
+        h = self.off_open(path.encode())
+        try:
+            nv, nhe = self.nv(h), self.nhe(h)
+            xyz = np.empty(3 * nv, np.float64)
+            VT = np.empty(nhe, np.uint32)
+            OT = np.empty(nhe, np.uint32)
+            EVT = np.empty(nv, np.uint32)
+            self.xyz(h, xyz)
+            self.tables(h, VT, OT, EVT)
+        finally:
+            self.free(h)
+        return xyz.reshape(-1, 3), VT, OT, EVT
 
 
 class RefMesh:

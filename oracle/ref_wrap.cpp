@@ -14,12 +14,14 @@
  *                                           src/geodesics_ptp.cpp:40-120
  *   - update_step                           src/geodesics_ptp.cpp:201-262
  *   - normalize_ptp                         src/geodesics_ptp.cpp:264-276
+ *   - che_off(file) (OFF reader)            src/che_off.cpp:28-79
  *
  * Built twice: once with real_t = double (the reference default) and once
  * with -DSINGLE_P (real_t = float).  The C entry points carry a suffix so
  * both libraries can be loaded into one process.
  */
 #include "che.h"
+#include "che_off.h"
 #include "geodesics_ptp.h"
 
 #include <cstring>
@@ -51,6 +53,30 @@ void * REFW(che_create)(const double * xyz, unsigned n_v, const unsigned * tri, 
 void REFW(che_free)(void * h)
 {
 	delete (che *) h;
+}
+
+/* Read an OFF file with the reference's reader (che_off). */
+void * REFW(off_open)(const char * path)
+{
+	return new gproshan::che_off(path);
+}
+
+unsigned REFW(che_n_vertices)(void * h)
+{
+	return (unsigned) ((che *) h)->n_vertices();
+}
+
+/* Copy the coordinates (3 per vertex) out of the mesh. */
+void REFW(che_xyz)(void * h, double * xyz)
+{
+	che * m = (che *) h;
+	for(index_t v = 0; v < m->n_vertices(); v++)
+	{
+		const gproshan::vertex & p = m->gt(v);
+		xyz[3 * v] = p.x;
+		xyz[3 * v + 1] = p.y;
+		xyz[3 * v + 2] = p.z;
+	}
 }
 
 unsigned REFW(che_n_half_edges)(void * h)
