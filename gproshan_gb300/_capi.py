@@ -117,6 +117,7 @@ SIGNATURES = {
     "gp_mesh_create_off": (C.c_int, [C.c_void_p, C.c_char_p, C.POINTER(C.c_void_p)]),
     "gp_che_build_device": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                       C.POINTER(C.c_int)]),
+    "gp_ctx_debug_barrier": (C.c_int, [C.c_void_p, C.c_uint32, C.c_uint32]),
     "gp_fps": (C.c_int, [C.c_void_p, C.c_void_p, C.c_void_p, C.c_uint32, C.c_uint32, C.c_uint64,
                          C.c_double, C.POINTER(gp_ptp_opts), _u32p, C.POINTER(C.c_double),
                          C.POINTER(C.c_double)]),

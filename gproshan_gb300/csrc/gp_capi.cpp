@@ -39,7 +39,7 @@ cudaError_t launch_plan(const FieldDev *fields, const FieldState *state, uint32_
                         uint32_t local_window, uint32_t *pred_big, float *cost, uint32_t *perm, cudaStream_t s);
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
-                       const QCtl *ctl, cudaStream_t s);
+                       const QCtl *ctl, uint32_t spin_limit, uint32_t phantom, cudaStream_t s);
 cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fields, QField *qf, QLine *cur,
                              QLine *done, QLine *sdone, QCtl *ctl, uint32_t ctas, uint32_t mode_req,
                              uint32_t min_queue, uint32_t tile, bool f64, bool clusters, cudaStream_t s);
@@ -70,6 +70,8 @@ struct gp_ctx {
 	uint32_t grid_ctas = 0;    // CTAs of the last grid launch
 	int queue_ctas[4] = {};    // CTAs of the work-queue launch (all resident) per variant
 	float *model = nullptr;    // cost-model parameters (device), or null
+	uint32_t dbg_spin = 0;     // grid-barrier poll limit (0: the default)
+	uint32_t dbg_phantom = 0;  // extra arrivals the grid barrier waits for (tests of the bounded wait)
 };
 
 struct gp_mesh {
@@ -551,7 +553,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		                              clusters, s));
 		GP_CUDA(ctx, launch_ptp(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_notok)),
 		                        reinterpret_cast<uint32_t *>(P(o_bar)), ctas, f64, clusters, ctx->steps,
-		                        ctx->steps_cap, dctl, s));
+		                        ctx->steps_cap, dctl, ctx->dbg_spin, ctx->dbg_phantom, s));
 		GP_CUDA(ctx, record(ctx->ph[4]));
 		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s));
 		cs.launches += 6;
@@ -1287,6 +1289,14 @@ void gp_plan_destroy(gp_plan *plan)
 	if(plan->graph) cudaGraphDestroy(plan->graph);
 	if(plan->ws) cudaFree(plan->ws);
 	delete plan;
+}
+
+gp_status gp_ctx_debug_barrier(gp_ctx *ctx, uint32_t spin_limit, uint32_t phantom_arrivals)
+{
+	if(!ctx) return GP_ERR_INVALID_ARG;
+	ctx->dbg_spin = spin_limit;
+	ctx->dbg_phantom = phantom_arrivals;
+	return GP_OK;
 }
 
 uint32_t gp_mlp_n_params(void) { return (uint32_t) MLP_NPARAM; }

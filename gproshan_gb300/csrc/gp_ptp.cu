@@ -715,6 +715,8 @@ struct GridArgs {
 	unsigned long long *steps;  // null, or 2 words per step: start time (ns), tiles << 32 | live fields
 	uint32_t steps_cap;
 	const QCtl *ctl;            // null, or the launch-mode choice (runs only if mode == GRID_LOCKSTEP)
+	uint32_t spin_limit;        // polls before a barrier wait gives up
+	uint32_t phantom;           // arrivals the barrier waits for beyond the launch's CTAs (0; tests)
 };
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -731,7 +733,7 @@ struct SchedSmem {
 // Counting barrier: arrival is a release-add, the wait an acquire spin until
 // every CTA of the step has arrived.  Bounded: gives up after SPIN_LIMIT polls
 // (error bit set, abort raised, caller returns).
-__device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t target)
+__device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t target, uint32_t limit)
 {
 	__shared__ uint32_t s_ok;
 	__syncthreads();
@@ -742,7 +744,7 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t target)
 		uint32_t spins = 0;
 		while(ld_acquire(bar) < target)
 		{
-			if(++spins > SPIN_LIMIT || ld_relaxed(bar + 1))
+			if(++spins > limit || ld_relaxed(bar + 1))
 			{
 				atomicOr(bar + 2, DEV_ERR_TIMEOUT);
 				atomicExch(bar + 1, 1u);
@@ -861,7 +863,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			// one atomic per warp that saw a failure, no block barrier per tile
 			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
 		}
-		if(!count_barrier(a.bar, gridDim.x * (step + 1))) return;
+		if(!count_barrier(a.bar, (gridDim.x + a.phantom) * (step + 1), a.spin_limit)) return;
 		// every CTA advances its own copy of every schedule
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
 		{
@@ -1585,14 +1587,14 @@ uint32_t ptp_grid_max_fields() { return GRID_MAX_FIELDS; }
 // notok: 3 * n_fields words; bar: 4 words.  Both zeroed here.
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
-                       const QCtl *ctl, cudaStream_t s)
+                       const QCtl *ctl, uint32_t spin_limit, uint32_t phantom, cudaStream_t s)
 {
 	if(!n_fields) return cudaSuccess;
 	cudaError_t e = cudaMemsetAsync(notok, 0, 3 * sizeof(uint32_t) * n_fields, s);
 	if(e == cudaSuccess) e = cudaMemsetAsync(bar, 0, 4 * sizeof(uint32_t), s);
 	if(e == cudaSuccess && steps) e = cudaMemsetAsync(steps, 0, 16 * (size_t) steps_cap, s);
 	if(e != cudaSuccess) return e;
-	GridArgs a{fields, state, n_fields, notok, bar, steps, steps_cap, ctl};
+	GridArgs a{fields, state, n_fields, notok, bar, steps, steps_cap, ctl, spin_limit ? spin_limit : SPIN_LIMIT, phantom};
 	void *args[] = {&a};
 	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters), dim3(ctas), dim3(NT), args,
 	                                   grid_smem_bytes(n_fields), s);

@@ -340,6 +340,16 @@ gp_status gp_mesh_create_off(gp_ctx *ctx, const char *path, gp_mesh **mesh);
 gp_status gp_che_build_device(gp_ctx *ctx, uint32_t n_vertices, uint32_t n_faces, const uint32_t *VT, uint32_t *OT,
                               uint32_t *EVT, int *manifold);
 
+/*
+ * Test hook for the bounded waits (no reference counterpart).  spin_limit:
+ * polls before the lockstep grid barrier gives up (0: the built-in limit,
+ * about a second or more); phantom_arrivals: arrivals the barrier waits for
+ * beyond the CTAs launched, so that with a value > 0 the wait cannot end and
+ * the call must report GP_ERR_DEVICE_TIMEOUT after spin_limit polls, with the
+ * context still usable.  Leave both 0 in normal use.
+ */
+gp_status gp_ctx_debug_barrier(gp_ctx *ctx, uint32_t spin_limit, uint32_t phantom_arrivals);
+
 /* normalize_ptp (src/geodesics_ptp.cpp:264-276) on a host array. */
 gp_status gp_normalize_ptp(gp_ctx *ctx, void *dist, gp_dtype dist_type, uint64_t n);
 

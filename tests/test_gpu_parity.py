@@ -195,6 +195,26 @@ def test_invalid_source_is_an_error_and_context_survives(gpu_ctx):
     assert d[0] == 0 and np.isfinite(d).all()
 
 
+def test_grid_barrier_wait_is_bounded_and_reported(gpu_ctx):
+    """A grid barrier that cannot complete (it waits for one arrival more
+    than the launch has CTAs, set through the test hook) gives up after its
+    poll limit: the call returns GP_ERR_DEVICE_TIMEOUT, nothing hangs, and the
+    context keeps working."""
+    from gproshan_gb300 import _capi, meshgen
+    m = dev_mesh(gpu_ctx, *meshgen.height_field(150, 2))
+    ref, _, _ = _capi.ptp(m, [0])
+    L = _capi.lib()
+    gpu_ctx.check(L.gp_ctx_debug_barrier(gpu_ctx.handle, 4000, 1), "gp_ctx_debug_barrier")
+    try:
+        with pytest.raises(_capi.GPError) as e:
+            _capi.ptp(m, [0], opts=_capi.make_opts(grid_kernel=_capi.GP_GRID_LOCKSTEP))
+        assert e.value.status == _capi.GP_ERR_DEVICE_TIMEOUT
+    finally:
+        gpu_ctx.check(L.gp_ctx_debug_barrier(gpu_ctx.handle, 0, 0), "gp_ctx_debug_barrier")
+    d, _, _ = _capi.ptp(m, [0])
+    assert np.array_equal(d, ref)
+
+
 @pytest.mark.parametrize("maker,src", [
     (lambda mg: mg.icosphere(4, 0.1, 1), [0]),
     (lambda mg: mg.height_field(96, 6), [5, 4000]),
