@@ -226,14 +226,7 @@ __device__ __forceinline__ void take32(const Nb32 &a, const Nb32 &b, Cand32 &bes
 	// cannot improve it: the edge fallback is >= min(t0, t1), and a causal
 	// planar solution lies beyond both t0 and t1 (delta = p - t0 > 0, rounding
 	// can only matter when delta is within ~1e-6 edge of 0).  Skip the solve.
-#ifndef GP_PRUNE
-#define GP_PRUNE 1
-#endif
-#if GP_PRUNE == 1
 	if(fminf(a.t, b.t) >= best.p) return;
-#elif GP_PRUNE == 2
-	if(__all_sync(__activemask(), fminf(a.t, b.t) >= best.p)) return;
-#endif
 	const Cand32 c = update32(a, b);
 	if(c.p < best.p)
 	{
@@ -363,7 +356,7 @@ __device__ __forceinline__ Nb32 make_nb(float4 pu, float2 t, float4 pv, uint32_t
 // <= FB are fetched at once, the neighbours in chunks of FC (bounded
 // registers, several loads in flight).  Returns the new (hi, lo) pair.
 #ifndef GP_FC
-#define GP_FC 4
+#define GP_FC 2
 #endif
 constexpr uint32_t FC = GP_FC;
 
