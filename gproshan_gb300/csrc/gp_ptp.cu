@@ -839,14 +839,17 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		}
 		if(!total) break;
 		uint32_t *flags = a.notok + (step % 3) * F;
+		uint32_t lo = 0;  // entry of the warp's current tile; tiles only move forward
 		for(uint32_t k = wid; k < total; k += warps)
 		{
-			uint32_t lo = 0, hi = G;  // last entry whose first tile <= k
-			while(hi - lo > 1)
+			// last entry whose first tile <= k: the lanes test 32 entries at once
+			for(;;)
 			{
-				const uint32_t mid = (lo + hi) >> 1;
-				if(ts[mid] <= k) lo = mid;
-				else hi = mid;
+				const uint32_t q = lo + lane;
+				const unsigned m = __ballot_sync(0xffffffffu, q < G && ts[q] <= k);
+				const uint32_t c = __popc(m);  // a prefix of the lanes
+				lo += c - 1;
+				if(c < 32) break;
 			}
 			const SchedSmem &x = fs[lo];
 			const uint32_t f = id[lo];
