@@ -26,7 +26,6 @@ cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uin
 cudaError_t launch_gather_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
                                 uint32_t total, bool f64, bool clusters, cudaStream_t s);
 cudaError_t launch_normalize(void *dist, bool f64, uint64_t n, unsigned long long *tmp, cudaStream_t s);
-int ptp_threads();
 int ptp_local_max_ctas(int device, bool f64, bool clusters);
 cudaError_t launch_classify(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
                             const uint32_t *pred_big, cudaStream_t s);
@@ -238,11 +237,10 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const bool given_tops = reqs[0].limits != nullptr;
 	const size_t tsz = 8;  // double (FP64 path) or a (hi, lo) float pair (FP32 path)
 	const size_t osz = out_type == GP_F64 ? sizeof(double) : sizeof(float);
-	const uint32_t NTH = (uint32_t) ptp_threads();
 
 	// ---- checks and layout -------------------------------------------------
 	std::vector<uint32_t> base(F + 1), vbase(F + 1), fbase(F + 1), sbase(F + 1);
-	uint64_t tot = 0, vtot = 0, ftot = 0, stot = 0, tiles = 0;
+	uint64_t tot = 0, vtot = 0, ftot = 0, stot = 0;
 	for(uint32_t f = 0; f < F; f++)
 	{
 		const Req &r = reqs[f];
@@ -278,7 +276,6 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		vtot += nv;
 		ftot += (uint64_t) r.mesh->dev.n_fan + (uint64_t) r.ns * r.mesh->dev.max_fan;
 		stot += r.ns;
-		tiles += (S + NTH - 1) / NTH + 1;
 	}
 	base[F] = (uint32_t) tot;
 	vbase[F] = (uint32_t) vtot;
@@ -314,11 +311,10 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	}
 
 	Carve cv;
-	const size_t o_fields = cv.add<FieldDev>(F), o_state = cv.add<FieldState>(F), o_plan = cv.add<PlanDev>(1);
-	const size_t o_act = cv.add<uint32_t>(F), o_ts = cv.add<uint32_t>(F + 1), o_aux = cv.add<uint32_t>(tiles + 2);
+	const size_t o_fields = cv.add<FieldDev>(F), o_state = cv.add<FieldState>(F);
 	const size_t o_sync = cv.add<GridSync>(2), o_base = cv.add<uint32_t>(F + 1), o_vbase = cv.add<uint32_t>(F + 1);
 	const size_t o_queue = cv.add<uint32_t>(4);
-	const size_t o_notok = cv.add<uint32_t>(3 * (size_t) F), o_bar = cv.add<uint32_t>(4);
+	const size_t o_notok = cv.add<uint32_t>(3 * (size_t) F), o_bar = cv.add<uint32_t>(GRID_BAR_WORDS);
 	const size_t o_feat = cv.add<float>((size_t) F * MLP_IN), o_pred = cv.add<float>((size_t) F * MLP_OUT);
 	const size_t o_pbig = cv.add<uint32_t>(F), o_cost = cv.add<float>(F), o_perm = cv.add<uint32_t>(F);
 	const size_t o_qf = cv.add<QField>(F), o_qcur = cv.add<QLine>((size_t) F * QUEUE_STRIPES);
@@ -462,21 +458,14 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 				GP_CUDA(ctx, cudaMemcpyAsync(dst, reqs[f].clusters, bytes,
 				                             out_dev ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
 			}
-	PlanDev hp{};
-	hp.act = reinterpret_cast<uint32_t *>(P(o_act));
-	hp.tile_start = reinterpret_cast<uint32_t *>(P(o_ts));
-	hp.tile_aux = reinterpret_cast<uint32_t *>(P(o_aux));
-	hp.cap_tiles = (uint32_t) tiles;
-	GP_CUDA(ctx, cudaMemcpyAsync(P(o_plan), &hp, sizeof(hp), cudaMemcpyHostToDevice, s));
-	uint64_t h2d = po + sizeof(hp), d2h = 0;
+	uint64_t h2d = po, d2h = 0;
 	if(clusters && !out_dev)
 		for(uint32_t f = 0; f < F; f++)
 			if(reqs[f].clusters) h2d += 4ull * reqs[f].mesh->nv;
-	GP_CUDA(ctx, cudaStreamSynchronize(s));  // hp lives on this stack frame
+	GP_CUDA(ctx, cudaStreamSynchronize(s));  // the staging buffer is reused by the next call
 
 	FieldDev *dF = reinterpret_cast<FieldDev *>(P(o_fields));
 	FieldState *dS = reinterpret_cast<FieldState *>(P(o_state));
-	PlanDev *dP = reinterpret_cast<PlanDev *>(P(o_plan));
 	GridSync *dSync = reinterpret_cast<GridSync *>(P(o_sync));
 	const uint32_t *dBase = reinterpret_cast<const uint32_t *>(P(o_base));
 	const uint32_t *dVbase = reinterpret_cast<const uint32_t *>(P(o_vbase));
@@ -649,7 +638,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		if(stage == Stage::ptp)
 			GP_CUDA(ctx, cudaMemcpy(hbar, P(o_bar), sizeof(hbar), cudaMemcpyDeviceToHost));
 		cs.grid_kernel = hctl.mode;
-		cs.sweeps_grid = hctl.mode == GRID_QUEUE ? hctl.progress : ctx->grid_ctas ? hbar[0] / ctx->grid_ctas : 0;
+		cs.sweeps_grid = hctl.mode == GRID_QUEUE ? hctl.progress : hbar[3];
 		cs.h2d_bytes = h2d;
 		cs.d2h_bytes = d2h + (stage == Stage::ptp ? 2 * sizeof(hbar) + sizeof(hctl) : 0);
 		ctx->last = cs;

@@ -64,55 +64,6 @@ __device__ __forceinline__ void st_relaxed(unsigned long long *p, unsigned long 
 	asm volatile("st.relaxed.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
 }
 
-// Grid-wide barrier of a cooperative launch.  The last CTA to arrive runs
-// `serial(...)` with all its threads while the others wait, then releases
-// them.  Returns false if the wait ran past SPIN_LIMIT or another CTA gave up;
-// the caller then leaves its loop (every CTA reads `abort` at its next
-// barrier, so the whole grid drains without hanging).
-template <class Serial>
-__device__ __forceinline__ bool grid_sync(GridSync *gs, uint32_t &gen, Serial &&serial)
-{
-	__shared__ uint32_t s_last;
-	__shared__ uint32_t s_ok;
-	__syncthreads();
-	if(threadIdx.x == 0)
-	{
-		__threadfence();
-		const uint32_t a = atom_add_acq_rel(&gs->count, 1u);
-		s_last = (a == gridDim.x - 1);
-		s_ok = 1;
-	}
-	__syncthreads();
-	if(s_last)
-	{
-		serial();
-		__syncthreads();
-		if(threadIdx.x == 0)
-		{
-			gs->count = 0;
-			__threadfence();
-			st_release(&gs->gen, gen + 1);
-		}
-	}
-	else if(threadIdx.x == 0)
-	{
-		uint32_t spins = 0;
-		while(ld_acquire(&gs->gen) == gen)
-		{
-			if(++spins > SPIN_LIMIT || ld_relaxed(&gs->abort))
-			{
-				atomicOr(&gs->err, DEV_ERR_TIMEOUT);
-				atomicExch(&gs->abort, 1u);
-				s_ok = 0;
-				break;
-			}
-			__nanosleep(128);
-		}
-	}
-	gen++;
-	__syncthreads();
-	return s_ok != 0;
-}
 
 // Exclusive scan of one value per thread over a block of NT threads.
 // *total (shared) receives the block sum.  Every thread must call it.

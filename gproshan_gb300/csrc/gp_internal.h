@@ -44,6 +44,10 @@ struct GridSync {
 // different L2 lines) and as many completion counters.  A cursor packs
 // epoch (12 bits, the field's sweep number mod 4096) | tiles (26) | next tile (26).
 constexpr uint32_t QUEUE_STRIPES = 4;
+// words of the lockstep grid launch's barrier block: [0] top arrivals, [1]
+// abort, [2] error bits, [3] steps, then 16 group counters on 128-byte lines
+constexpr uint32_t GRID_BAR_GROUPS = 16;
+constexpr uint32_t GRID_BAR_WORDS = 32 * (GRID_BAR_GROUPS + 1);
 constexpr uint32_t GRID_NONE = 0, GRID_LOCKSTEP = 1, GRID_QUEUE = 2;
 
 struct alignas(128) QLine {
@@ -126,31 +130,16 @@ struct FieldDev {
 // Mutable per-field state of the persistent launches.
 struct FieldState {
 	// toplesets
-	uint32_t level;      // ring index of the current frontier
 	uint32_t n_limits;   // |limits| once the BFS is finished
 	uint32_t bfs_live;   // 1 while the BFS of this field runs
 	uint32_t status;     // DEV_ERR_* of this field
-	uint32_t bfs_next;   // size of the ring found by the current BFS level
 	// PTP schedule (run_ptp_gpu, src/cuda/geodesics_ptp.cu:198-229)
-	uint32_t i, j, d, iter, max_iter, n_iter, live, notok;
-	uint32_t win_s, win_e, chk_e, nr;
+	uint32_t i, j, d, iter, max_iter, n_iter, live;
+	uint32_t win_s, win_e, chk_e, nr;  // current window, check-ring end, reached vertices
 	uint32_t big;        // 1: swept by the grid-wide launch, 0: by one CTA
-	uint32_t bound;      // largest window the schedule can open: max_j limits[j] - limits[j/2]
 	unsigned long long relax;
 };
 
-// Host-visible description of a batch plan (all in one device allocation).
-struct PlanDev {
-	uint32_t n_act;        // active fields this step
-	uint32_t total_tiles;  // tiles of this step
-	uint32_t live;         // any field still running
-	uint32_t step;         // steps taken
-	uint32_t *act;         // F: active field ids
-	uint32_t *tile_start;  // F + 1: first tile of each active field
-	uint32_t *tile_aux;    // per-tile scratch (BFS tile counts / bases)
-	uint32_t cap_tiles;
-	uint32_t pad;
-};
 
 // ------------------------------------------------------------------
 // Kernel entry points implemented in the .cu files (all asynchronous on `s`).

@@ -12,10 +12,13 @@
 // to one sentinel id (distance INF), which reproduces the reference's view of
 // them: they never enter a window and read as INF.
 //
-// Sweep.  One cooperative launch runs every sweep of every live field.  Each
-// step, CTAs walk the tiles of all live windows (relax + the ring-i test);
-// the last CTA to reach the grid barrier applies the reference's schedule
-// rule to each field and lays out the next step's tiles.  No host round trip.
+// Sweeps.  Every field starts on one CTA (ptp_local_kernel), which runs its
+// sweeps with CTA barriers as long as the windows stay small; a field whose
+// window outgrows local_window is handed, mid-schedule, to the grid-wide
+// launch: ptp_kernel (lockstep: one sweep of every live field per step, a
+// counting grid barrier, every CTA applying the reference's schedule rule to
+// its own copy of the schedules) or ptp_queue_kernel (work queue: per-field
+// claims and completions, no grid barrier).  No host round trip.
 #include <cfloat>
 #include <cmath>
 #include <type_traits>
@@ -506,9 +509,8 @@ labels:
 }
 
 // ---------------------------------------------------------------------------
-// classify: reset every field's schedule state (i = 1, j = 2, d = 0) and
-// record the largest window its schedule could open, max_j limits[j] -
-// limits[j/2] (statistics).  Every field starts on one CTA.
+// classify: reset every field's schedule state (i = 1, j = 2, d = 0).  Every
+// field starts on one CTA, unless the cost model predicted it outgrows one.
 // ---------------------------------------------------------------------------
 __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
                                 const uint32_t *pred_big)
@@ -518,12 +520,8 @@ __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 	const FieldDev &F = fields[warp];
 	FieldState &st = state[warp];
 	const uint32_t nl = st.n_limits;
-	uint32_t bound = 0;
-	for(uint32_t j = 2 + lane; j < nl; j += 32) bound = max(bound, F.limits[j] - F.limits[j >> 1]);
-	for(int o = 16; o; o >>= 1) bound = max(bound, __shfl_xor_sync(0xffffffffu, bound, o));
 	if(lane == 0)
 	{
-		st.bound = bound;
 		st.big = 0;
 		st.nr = nl ? F.limits[nl - 1] : 0;
 		st.i = 1;
@@ -531,7 +529,6 @@ __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 		st.d = 0;
 		st.iter = 0;
 		st.n_iter = 0;
-		st.notok = 0;
 		st.live = 0;
 		st.relax = 0;
 		st.max_iter = F.max_iter ? F.max_iter : (nl << 1);
@@ -704,7 +701,7 @@ struct GridArgs {
 	FieldState *state;
 	uint32_t n_fields;
 	uint32_t *notok;  // 3 * n_fields, zeroed before the launch
-	uint32_t *bar;    // [0] arrivals (zeroed), [1] abort, [2] error bits
+	uint32_t *bar;    // GRID_BAR_WORDS, zeroed: see count_barrier
 	unsigned long long *steps;  // null, or 2 words per step: start time (ns), tiles << 32 | live fields
 	uint32_t steps_cap;
 	const QCtl *ctl;            // null, or the launch-mode choice (runs only if mode == GRID_LOCKSTEP)
@@ -723,17 +720,27 @@ struct SchedSmem {
 	uint32_t i, j, d, iter, n_iter, max_iter, nl, live, win_s, win_e, chk_e, grid;
 };
 
-// Counting barrier: arrival is a release-add, the wait an acquire spin until
-// every CTA of the step has arrived.  Bounded: gives up after SPIN_LIMIT polls
-// (error bit set, abort raised, caller returns).
-__device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t target, uint32_t limit)
+// Counting barrier in two levels: a CTA arrives on its group's counter
+// (acquire-release add; GRID_BAR_GROUPS groups, one 128-byte line each, so the
+// arrivals are spread over several L2 slices), the last CTA of a group
+// arrives on the top counter (release add), and every CTA waits for all
+// groups with an acquire spin.  Bounded: gives up after `limit` polls (error
+// bit set, abort raised, caller returns).  bar: [0] top arrivals, [1] abort,
+// [2] error bits, [3] steps; group g counts at bar[32 * (g + 1)].
+
+__device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint32_t limit, uint32_t phantom)
 {
 	__shared__ uint32_t s_ok;
 	__syncthreads();
 	if(threadIdx.x == 0)
 	{
 		s_ok = 1;
-		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+		const uint32_t groups = min(GRID_BAR_GROUPS, gridDim.x), g = blockIdx.x % groups;
+		const uint32_t members = gridDim.x / groups + (g < gridDim.x % groups ? 1u : 0u);
+		const uint32_t old = atom_add_acq_rel(bar + 32 * (g + 1), 1u);
+		if(old + 1 == members * (step + 1))
+			asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+		const uint32_t target = (groups + phantom) * (step + 1);
 		uint32_t spins = 0;
 		while(ld_acquire(bar) < target)
 		{
@@ -837,7 +844,11 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			a.steps[2 * step] = global_ns();
 			a.steps[2 * step + 1] = ((unsigned long long) total << 32) | live;
 		}
-		if(!total) break;
+		if(!total)
+		{
+			if(blockIdx.x == 0 && threadIdx.x == 0) a.bar[3] = step;
+			break;
+		}
 		uint32_t *flags = a.notok + (step % 3) * F;
 		uint32_t lo = 0;  // entry of the warp's current tile; tiles only move forward
 		for(uint32_t k = wid; k < total; k += warps)
@@ -859,7 +870,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			// one atomic per warp that saw a failure, no block barrier per tile
 			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
 		}
-		if(!count_barrier(a.bar, (gridDim.x + a.phantom) * (step + 1), a.spin_limit)) return;
+		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom)) return;
 		// every CTA advances its own copy of every schedule
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
 		{
@@ -1576,7 +1587,6 @@ cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fie
 	return cudaLaunchKernel(ptp_queue_ptr(f64, clusters), dim3(ctas), dim3(NT), args, 0, s);
 }
 
-int ptp_threads() { return NT; }
 
 uint32_t ptp_grid_max_fields() { return GRID_MAX_FIELDS; }
 
@@ -1587,7 +1597,7 @@ cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, u
 {
 	if(!n_fields) return cudaSuccess;
 	cudaError_t e = cudaMemsetAsync(notok, 0, 3 * sizeof(uint32_t) * n_fields, s);
-	if(e == cudaSuccess) e = cudaMemsetAsync(bar, 0, 4 * sizeof(uint32_t), s);
+	if(e == cudaSuccess) e = cudaMemsetAsync(bar, 0, GRID_BAR_WORDS * sizeof(uint32_t), s);
 	if(e == cudaSuccess && steps) e = cudaMemsetAsync(steps, 0, 16 * (size_t) steps_cap, s);
 	if(e != cudaSuccess) return e;
 	GridArgs a{fields, state, n_fields, notok, bar, steps, steps_cap, ctl, spin_limit ? spin_limit : SPIN_LIMIT, phantom};

@@ -26,11 +26,17 @@ namespace gp {
 
 namespace {
 
-constexpr int BT = 1024;  // threads of a BFS CTA
+#ifndef GP_BT
+#define GP_BT 1024
+#endif
+constexpr int BT = GP_BT;  // threads of a BFS CTA
 
 // Frontier vertices whose link rows a thread keeps in registers between the
 // two passes of a level, and the shared-memory copy of the frontier.
-constexpr uint32_t KB = 2;
+#ifndef GP_KB
+#define GP_KB 2
+#endif
+constexpr uint32_t KB = GP_KB;
 constexpr uint32_t SF = BT * KB;
 
 __device__ __forceinline__ uint32_t slot_of(const uint4 &a, const uint4 &b, uint32_t q)
@@ -86,7 +92,7 @@ __device__ __forceinline__ uint32_t owned(const FieldDev &F, uint32_t p, uint32_
 	return mask;
 }
 
-__global__ void __launch_bounds__(BT) bfs_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields,
+__global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields,
                                                  uint32_t *queue)
 {
 	__shared__ uint32_t s_f;
@@ -420,9 +426,7 @@ __global__ void bfs_seed_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 	if(f >= n_fields) return;
 	FieldDev &F = fields[f];
 	FieldState &st = state[f];
-	st.level = 0;
 	st.status = 0;
-	st.bfs_next = 0;
 	for(uint32_t s = 0; s < F.ns; s++)
 		if(F.src[s] >= F.m.nv)
 		{
