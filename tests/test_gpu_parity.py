@@ -98,6 +98,54 @@ def test_larger_meshes_against_oracle(gpu_ctx, oracle_lib, maker, src):
     assert oracle_lib.max_rel_err(d32, ref["dist"]) <= REL_TOL_F32
 
 
+def _degenerate_mesh():
+    """A height field with collinear vertices (zero-area triangles) and
+    coincident vertices (zero-length edges)."""
+    from gproshan_gb300 import meshgen
+    xyz, tri = meshgen.height_field(40, 3)
+    n = 40
+    for r in range(5, 35, 6):
+        for c in range(5, 35, 7):
+            v = r * n + c
+            xyz[v] = 0.5 * (xyz[v - 1] + xyz[v + 1])
+    for r in range(8, 32, 9):
+        v = r * n + 20
+        xyz[v] = xyz[v + n]
+    return xyz, tri
+
+
+def test_degenerate_triangles_follow_the_reference(gpu_ctx, oracle_lib):
+    """Zero-area triangles give NaN candidates that the reference ignores (INF
+    inputs still take the edge fallback), zero-length edges give zero
+    fallbacks: the FP64 path matches bit for bit, the FP32 path within tol."""
+    from gproshan_gb300 import _capi
+    xyz, tri = _degenerate_mesh()
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    src = [0, 777]
+    _, s_o, l_o = oracle_lib.toplesets(om, src)
+    ref64 = oracle_lib.ptp(om, src, l_o, s_o)
+    d64, _, st = _capi.ptp(m, src, dtype=np.float64, precision=_capi.GP_F64)
+    assert st.n_iter == ref64["n_iter"] and np.array_equal(d64, ref64["dist"])
+    ref = oracle_lib.ptp(om, src, l_o, s_o, xyz=xyz.astype(np.float32).astype(np.float64))
+    d32, _, st32 = _capi.ptp(m, src)
+    assert np.isfinite(d32).all() and st32.n_iter == ref["n_iter"]
+    assert oracle_lib.max_rel_err(d32, ref["dist"]) <= REL_TOL_F32
+
+
+def test_batches_longer_than_one_device_pass(gpu_ctx):
+    """More fields than one device pass holds (2048): the call is chunked and
+    every field equals its single-field result."""
+    from gproshan_gb300 import _capi, meshgen
+    m = dev_mesh(gpu_ctx, *meshgen.icosphere(2, 0.1, 4))
+    rng = np.random.default_rng(3)
+    srcs = [rng.choice(m.n_vertices, size=1 + k % 2, replace=False) for k in range(2100)]
+    d, st, _ = _capi.ptp_batch(gpu_ctx, [m] * len(srcs), srcs)
+    for k in (0, 1, 2047, 2048, 2099):
+        d1, _, s1 = _capi.ptp(m, srcs[k])
+        assert np.array_equal(d1, d[k]) and s1.n_iter == st[k].n_iter, k
+
+
 def test_duplicate_and_isolated_sources(gpu_ctx, oracle_lib):
     from gproshan_gb300 import _capi
     g = dict(np.load(__import__("os").path.join(__import__("conftest").GOLDEN, "grid_hole.npz")))
