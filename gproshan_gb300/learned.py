@@ -108,33 +108,40 @@ def predict(ctx, features, params, bf16: bool = True):
 
 # ---- training workload --------------------------------------------------------
 
-def training_meshes(seed: int = 0, n: int = 48):
-    """Seeded mix of the mesh families the library is used on: icospheres,
-    height fields, strips, tori and bump fields, from a few hundred to ~250k
-    vertices."""
+def training_meshes(seed: int = 0, n: int = 48, families: str = "mixed"):
+    """Seeded meshes, one at a time.  ``mixed``: icospheres, height fields,
+    strips, tori and bump fields (a few hundred to ~250k vertices);
+    ``configs``: the families of the benchmark configurations, icospheres
+    subdivided 3-6 times and height fields 64^2-512^2."""
     rng = np.random.default_rng(seed)
-    out = []
     for k in range(n):
         s = int(rng.integers(0, 1 << 30))
+        if families == "configs":
+            if k % 2 == 0:
+                lv = int(rng.integers(3, 7))
+                yield (f"ico{lv}", *meshgen.icosphere(lv, 0.1, s))
+            else:
+                m = int(round(2.0 ** rng.uniform(6, 9)))
+                yield (f"grid{m}", *meshgen.height_field(m, s))
+            continue
         kind = k % 5
         if kind == 0:
             lv = int(rng.integers(2, 8))
-            out.append((f"ico{lv}", *meshgen.icosphere(lv, 0.1, s)))
+            yield (f"ico{lv}", *meshgen.icosphere(lv, 0.1, s))
         elif kind == 1:
             m = int(round(2.0 ** rng.uniform(4, 9)))
-            out.append((f"grid{m}", *meshgen.height_field(m, s)))
+            yield (f"grid{m}", *meshgen.height_field(m, s))
         elif kind == 2:
             w = int(rng.integers(3, 17))
             ln = int(round(2.0 ** rng.uniform(6, 12)))
-            out.append((f"strip{w}x{ln}", *meshgen.height_field(w, s, cols=ln)))
+            yield (f"strip{w}x{ln}", *meshgen.height_field(w, s, cols=ln))
         elif kind == 3:
             a = int(round(2.0 ** rng.uniform(4, 8)))
             b = int(round(2.0 ** rng.uniform(4, 9)))
-            out.append((f"torus{a}x{b}", *meshgen.torus(a, b, seed=s)))
+            yield (f"torus{a}x{b}", *meshgen.torus(a, b, seed=s))
         else:
             m = int(round(2.0 ** rng.uniform(4, 9)))
-            out.append((f"bump{m}", *meshgen.bump_field(m, s)))
-    return out
+            yield (f"bump{m}", *meshgen.bump_field(m, s))
 
 
 def random_sources(rng, nv: int):
@@ -151,47 +158,82 @@ def collect(ctx, meshes, sources_list):
     return X, T, ok
 
 
-def build_dataset(ctx, seed: int = 0, n_meshes: int = 48, fields_per_mesh: int = 16):
-    """(X, T, mesh index) of the fields that ran sweeps."""
+def build_dataset(ctx, seed: int = 0, n_meshes: int = 48, fields_per_mesh: int = 16, families: str = "mixed",
+                  chunk: int = 32):
+    """(X, T, mesh index) of the fields that ran sweeps; meshes are generated,
+    uploaded, solved and freed `chunk` at a time."""
     rng = np.random.default_rng(seed + 1)
+    Xs, Ts, Gs = [], [], []
     dms, srcs, gid = [], [], []
-    for g, (_, xyz, tri) in enumerate(training_meshes(seed, n_meshes)):
+
+    def flush():
+        if srcs:
+            X, T, ok = collect(ctx, dms, srcs)
+            Xs.append(X[ok])
+            Ts.append(T[ok])
+            Gs.append(np.asarray(gid)[ok])
+        for m in {id(d): d for d in dms}.values():
+            m.close()
+        dms.clear()
+        srcs.clear()
+        gid.clear()
+
+    for g, (_, xyz, tri) in enumerate(training_meshes(seed, n_meshes, families)):
         dm = _capi.DeviceMesh(ctx, xyz, tri)
         for _ in range(fields_per_mesh):
             dms.append(dm)
             srcs.append(random_sources(rng, dm.n_vertices))
             gid.append(g)
-    Xs, Ts, oks = [], [], []
-    for a in range(0, len(srcs), 512):
-        X, T, ok = collect(ctx, dms[a:a + 512], srcs[a:a + 512])
-        Xs.append(X)
-        Ts.append(T)
-        oks.append(ok)
-    X, T, ok = np.concatenate(Xs), np.concatenate(Ts), np.concatenate(oks)
-    return X[ok], T[ok], np.asarray(gid)[ok]
+        if (g + 1) % chunk == 0:
+            flush()
+    flush()
+    return np.concatenate(Xs), np.concatenate(Ts), np.concatenate(Gs)
+
+
+def torus_eval(ctx, params):
+    """Mean |error| (log-sweeps, log-relaxations) on the 1M-vertex anisotropic
+    torus: 16 single-source fields and one field with all 16 sources."""
+    xyz, tri = meshgen.torus(400, 2500, seed=0)
+    m = _capi.DeviceMesh(ctx, xyz, tri)
+    s16 = np.random.default_rng(4).choice(len(xyz), 16, replace=False).astype(np.uint32)
+    srcs = [[int(x)] for x in s16] + [s16]
+    X, T, ok = collect(ctx, [m] * len(srcs), srcs)
+    m.close()
+    Y = predict(ctx, X[ok], params)
+    return np.abs(Y - T[ok]).mean(0)
 
 
 def main(argv=None):
     ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
     ap.add_argument("--out", default=DEFAULT_MODEL)
     ap.add_argument("--seed", type=int, default=0)
-    ap.add_argument("--meshes", type=int, default=60)
-    ap.add_argument("--fields", type=int, default=16)
+    ap.add_argument("--config-meshes", type=int, default=2000,
+                    help="meshes of the benchmark families (icospheres, height fields)")
+    ap.add_argument("--config-fields", type=int, default=4)
+    ap.add_argument("--mixed-meshes", type=int, default=60, help="meshes of the wider mix (strips, tori, bumps, ...)")
+    ap.add_argument("--mixed-fields", type=int, default=16)
     ap.add_argument("--epochs", type=int, default=6000)
     ap.add_argument("--lr", type=float, default=3e-3)
     a = ap.parse_args(argv)
     ctx = _capi.Context(0)
-    X, T, g = build_dataset(ctx, a.seed, a.meshes, a.fields)
-    # validation on whole held-out meshes (every fifth), not on other fields of training meshes
+    X1, T1, g1 = build_dataset(ctx, a.seed, a.config_meshes, a.config_fields, "configs")
+    X2, T2, g2 = build_dataset(ctx, a.seed + 7, a.mixed_meshes, a.mixed_fields, "mixed")
+    X = np.concatenate([X1, X2])
+    T = np.concatenate([T1, T2])
+    g = np.concatenate([g1, g2 + a.config_meshes])
+    # validation on whole held-out meshes (one group of five in five), not on
+    # other fields of training meshes
     held = (g // 5) % 5 == 4
     va, tr = np.flatnonzero(held), np.flatnonzero(~held)
-    nval = len(va)
     params, losses = fit(ctx, X[tr], T[tr], a.epochs, a.lr, a.seed)
     Y = predict(ctx, X[va], params)
     mae = np.abs(Y - T[va]).mean(0)
-    print(f"samples train {len(tr)} val {nval}; final train loss {losses[-1]:.4f}; "
-          f"val mean |err| log-sweeps {mae[0]:.3f} log-relax {mae[1]:.3f}")
-    save(a.out, params, val_mae=mae, n_train=len(tr), n_val=nval, seed=a.seed)
+    tmae = torus_eval(ctx, params)
+    print(f"meshes {a.config_meshes} + {a.mixed_meshes}; samples train {len(tr)} val {len(va)}; "
+          f"final train loss {losses[-1]:.4f}; val mean |err| log-sweeps {mae[0]:.3f} log-relax {mae[1]:.3f}; "
+          f"torus (held-out family) {tmae[0]:.3f} / {tmae[1]:.3f}")
+    save(a.out, params, val_mae=mae, torus_mae=tmae, n_train=len(tr), n_val=len(va), seed=a.seed,
+         meshes=np.array([a.config_meshes, a.mixed_meshes]))
     print(a.out)
 
 
