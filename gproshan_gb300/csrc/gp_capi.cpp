@@ -774,7 +774,6 @@ gp_status gp_ctx_step_trace(gp_ctx *ctx, uint32_t cap, uint64_t *out, uint32_t *
 	{
 		// (re)arm: record up to cap steps of the following calls' grid launches
 		if(ctx->steps) cudaFree(ctx->steps);
-	if(ctx->model) cudaFree(ctx->model);
 		ctx->steps = nullptr;
 		ctx->steps_cap = 0;
 		if(cap)
