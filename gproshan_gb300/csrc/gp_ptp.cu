@@ -31,7 +31,7 @@ namespace gp {
 namespace {
 
 #ifndef GP_NT
-#define GP_NT 256
+#define GP_NT 1024
 #endif
 constexpr int NT = GP_NT;  // threads of a grid-launch CTA
 
@@ -781,7 +781,7 @@ __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uin
 
 template <typename T, bool CL>
 #ifndef GP_GRID_MINB
-#define GP_GRID_MINB 3
+#define GP_GRID_MINB 1
 #endif
 __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 {
@@ -797,7 +797,6 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	__shared__ uint32_t s_G;
 	const uint32_t lane = threadIdx.x & 31;
 	constexpr uint32_t TV = 32;  // window vertices per tile: one warp's worth
-	const uint32_t warps = gridDim.x * (NT / 32), wid = blockIdx.x * (NT / 32) + (threadIdx.x >> 5);
 
 	if(threadIdx.x == 0) s_G = 0;
 	__syncthreads();
@@ -851,8 +850,20 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		}
 		uint32_t *flags = a.notok + (step % 3) * F;
 		uint32_t lo = 0;  // entry of the warp's current tile; tiles only move forward
-		for(uint32_t k = wid; k < total; k += warps)
+		// CTA b (one per SM) owns tiles b, b + C, b + 2C, ...; its 32 warps take
+		// them in order from a shared counter, so they all finish within about
+		// one tile of each other (dealt statically, warps of one SM finished
+		// ~10 us apart in a heavy step: the scheduler favours some warps)
+		__shared__ uint32_t s_tile;
+		if(threadIdx.x == 0) s_tile = 0;
+		__syncthreads();
+		for(;;)
 		{
+			uint32_t r = 0;
+			if(lane == 0) r = atomicAdd(&s_tile, 1u);
+			r = __shfl_sync(0xffffffffu, r, 0);
+			const uint32_t k = blockIdx.x + r * gridDim.x;
+			if(k >= total) break;
 			// last entry whose first tile <= k: the lanes test 32 entries at once
 			for(;;)
 			{
