@@ -759,10 +759,30 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint
 
 // Tiles of every live window (TV window vertices per tile); ts[G] = total.
 template <uint32_t TV>
-__device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uint32_t G)
+__device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uint32_t G, uint32_t *s_tile)
 {
+	if(G <= NT)
+	{
+		// one round (the usual case): one block scan, the tile counter reset with it
+		const uint32_t q = threadIdx.x;
+		const uint32_t tiles = q < G && fs[q].live ? (fs[q].win_e - fs[q].win_s + TV - 1) / TV : 0u;
+		uint32_t tot;
+		const uint32_t ex = block_exclusive_scan<NT>(tiles, &tot);
+		if(q < G) ts[q] = ex;
+		if(q == 0)
+		{
+			ts[G] = tot;
+			*s_tile = 0;
+		}
+		__syncthreads();
+		return;
+	}
 	__shared__ uint32_t carry;
-	if(threadIdx.x == 0) carry = 0;
+	if(threadIdx.x == 0)
+	{
+		carry = 0;
+		*s_tile = 0;
+	}
 	__syncthreads();
 	for(uint32_t base = 0; base < G; base += NT)
 	{
@@ -831,7 +851,8 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		__syncthreads();
 	}
 	const uint32_t G = s_G;
-	grid_plan<TV>(fs, ts, G);
+	__shared__ uint32_t s_tile;  // the CTA's next tile (see the step loop)
+	grid_plan<TV>(fs, ts, G, &s_tile);
 
 	for(uint32_t step = 0;; step++)
 	{
@@ -851,12 +872,10 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		uint32_t *flags = a.notok + (step % 3) * F;
 		uint32_t lo = 0;  // entry of the warp's current tile; tiles only move forward
 		// CTA b (one per SM) owns tiles b, b + C, b + 2C, ...; its 32 warps take
-		// them in order from a shared counter, so they all finish within about
-		// one tile of each other (dealt statically, warps of one SM finished
-		// ~10 us apart in a heavy step: the scheduler favours some warps)
-		__shared__ uint32_t s_tile;
-		if(threadIdx.x == 0) s_tile = 0;
-		__syncthreads();
+		// them in order from a shared counter (reset by grid_plan), so they all
+		// finish within about one tile of each other (dealt statically, warps of
+		// one SM finished ~10 us apart in a heavy step: the scheduler favours
+		// some warps)
 		for(;;)
 		{
 			uint32_t r = 0;
@@ -914,7 +933,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			rx[q] = st.relax;
 		}
 		__syncthreads();
-		grid_plan<TV>(fs, ts, G);
+		grid_plan<TV>(fs, ts, G, &s_tile);
 	}
 	if(blockIdx.x == 0)
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
