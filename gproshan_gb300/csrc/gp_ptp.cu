@@ -717,8 +717,46 @@ __device__ __forceinline__ unsigned long long global_ns()
 }
 
 struct SchedSmem {
-	uint32_t i, j, d, iter, n_iter, max_iter, nl, live, win_s, win_e, chk_e, grid;
+	uint32_t i, j, d, iter, n_iter, max_iter, nl, live, win_s, win_e, chk_e;
+	// limits the next window may need, loaded while this step runs:
+	// [0..1] from i' = max(i, j'/2) (ring test failed), [2..3] from
+	// max(i + 1, j'/2) (passed), [4] at j' (the next j)
+	uint32_t nx[5];
 };
+
+__device__ __forceinline__ void prefetch_limits(const FieldDev &F, SchedSmem &x)
+{
+	if(!x.live) return;
+	const uint32_t j1 = x.j < x.nl - 1 ? x.j + 1 : x.j;
+	const uint32_t ia = max(x.i, j1 >> 1), ib = max(x.i + 1, j1 >> 1);
+	const uint32_t *lim = F.limits;
+	x.nx[0] = ia < x.nl ? lim[ia] : 0u;
+	x.nx[1] = ia + 1 < x.nl ? lim[ia + 1] : 0u;
+	x.nx[2] = ib < x.nl ? lim[ib] : 0u;
+	x.nx[3] = ib + 1 < x.nl ? lim[ib + 1] : 0u;
+	x.nx[4] = lim[j1];
+}
+
+// open_sweep with the prefetched limits; `passed` = the ring test of the
+// sweep just closed passed (close_sweep advanced i)
+__device__ __forceinline__ void open_sweep_cached(const FieldDev *F, FieldState &st, const SchedSmem &x, bool passed)
+{
+	if(st.i < st.j && st.iter < st.max_iter)
+	{
+		st.iter++;
+		if(st.i < (st.j >> 1)) st.i = st.j >> 1;
+		st.win_s = passed ? x.nx[2] : x.nx[0];
+		st.chk_e = passed ? x.nx[3] : x.nx[1];
+		st.win_e = x.nx[4];
+		st.live = 1;
+		if(F && F->trace && st.n_iter < F->trace_cap)
+		{
+			F->trace[2 * st.n_iter] = st.i;
+			F->trace[2 * st.n_iter + 1] = st.j;
+		}
+	}
+	else st.live = 0;
+}
 
 // Counting barrier in two levels: a CTA arrives on its group's counter
 // (acquire-release add; GRID_BAR_GROUPS groups, one 128-byte line each, so the
@@ -832,7 +870,6 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			const uint32_t q = s_G + ex;
 			SchedSmem &x = fs[q];
 			id[q] = f;
-			x.grid = 1;
 			x.live = 1;
 			x.i = g.i;
 			x.j = g.j;
@@ -853,6 +890,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	const uint32_t G = s_G;
 	__shared__ uint32_t s_tile;  // the CTA's next tile (see the step loop)
 	grid_plan<TV>(fs, ts, G, &s_tile);
+	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
 
 	for(uint32_t step = 0;; step++)
 	{
@@ -919,8 +957,9 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			st.win_s = x.win_s;
 			st.win_e = x.win_e;
 			st.relax = rx[q];
-			close_sweep(st, !ldcg(flags + f));
-			open_sweep(a.fields[f], st, blockIdx.x == 0);
+			const bool passed = !ldcg(flags + f);
+			close_sweep(st, passed);
+			open_sweep_cached(blockIdx.x == 0 ? a.fields + f : nullptr, st, x, passed);
 			x.i = st.i;
 			x.j = st.j;
 			x.d = st.d;
@@ -934,6 +973,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		}
 		__syncthreads();
 		grid_plan<TV>(fs, ts, G, &s_tile);
+		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
 	}
 	if(blockIdx.x == 0)
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
