@@ -14,7 +14,7 @@ events on the library's stream.
              outputs resident in HBM;
 * plain   -- the same fields one gp_ptp_batch call each (the single-field GPU
              PTP), same GPU, same kernels;
-* e2e     -- batched through the C ABI with HOST buffers: sources copied in,
+* e2e     -- batched through the C ABI with HOST buffers (page-locked): sources copied in,
              distances copied out every step (meshes stay resident, as a
              reference `che` does between calls);
 * roofline -- the sweep launch's algorithmic bytes (48 per relaxation) over
@@ -289,7 +289,10 @@ def run_gpu(args, rank, world, local):
 
     # e2e with host buffers through the same C entry point
     src_pinned = torch.from_numpy(src_host.view(np.int32)).pin_memory()
-    host_out = [np.empty(n, np.float32) for n in nv]
+    # results land in page-locked host memory (one buffer, per-field views)
+    out_pinned = torch.empty(int(voff[-1]), dtype=torch.float32).pin_memory()
+    out_np = out_pinned.numpy()
+    host_out = [out_np[voff[k]:voff[k + 1]] for k in range(F)]
     host_fields = field_array(False, host_out, src_pinned.numpy().view(np.uint32))
 
     def e2e():
