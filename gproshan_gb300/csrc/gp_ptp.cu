@@ -132,14 +132,11 @@ __device__ __forceinline__ Cand32 update32(const Nb32 &a, const Nb32 &b)
 	c.t = planar ? a.t : ft;
 	c.x = planar ? delta : fx;
 	c.te = planar ? a.te : fe;
-	if(!(A2 > 0.f)) c.p = NAN;  // degenerate triangle: ignored
-	if(a.t == INFINITY || b.t == INFINITY)
-	{
-		c.p = fb;
-		c.t = ft;
-		c.x = fx;
-		c.te = fe;
-	}
+	// An INF input never passes the planar test (dt is +-INF, so r = -INF;
+	// or both INF, dt and the test are NaN), so the candidate is already the
+	// edge fallback then.  A degenerate triangle (A == 0) yields NaN and is
+	// ignored, except with an INF input: the reference checks INF first.
+	if(!(A2 > 0.f) && fmaxf(a.t, b.t) != INFINITY) c.p = NAN;
 	return c;
 }
 
