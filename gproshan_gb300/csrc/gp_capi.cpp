@@ -408,6 +408,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			d.max_iter = o.max_iter;
 			d.round_coords = o.round_coords ? 1u : 0u;
 			d.tol = o.tol > 0 ? o.tol : GP_PTP_TOL;
+			d.tol32 = (float) d.tol;
 		}
 		if(given_tops) hs[f].n_limits = r.nl;
 	}

@@ -125,6 +125,7 @@ struct FieldDev {
 	uint32_t max_iter;        // 0: 2 * n_limits
 	uint32_t round_coords;    // FP64 path on the float-rounded coordinates
 	double tol;
+	float tol32;              // tol rounded to float (the FP32 path's ring test)
 };
 
 // Mutable per-field state of the persistent launches.

@@ -222,11 +222,8 @@ constexpr uint32_t FB = 8;
 template <bool CL, bool COH>
 __device__ __forceinline__ void take32(const Nb32 &a, const Nb32 &b, Cand32 &best, uint32_t &lab, const uint32_t *Co)
 {
-	// A triangle whose two neighbours are both no closer than the current best
-	// cannot improve it: the edge fallback is >= min(t0, t1), and a causal
-	// planar solution lies beyond both t0 and t1 (delta = p - t0 > 0, rounding
-	// can only matter when delta is within ~1e-6 edge of 0).  Skip the solve.
-	if(fminf(a.t, b.t) >= best.p) return;
+	// Every triangle is solved: a skip test on min(t0, t1) >= best costs more
+	// issue slots than the solves it saves (the update is branch-free).
 	const Cand32 c = update32(a, b);
 	if(c.p < best.p)
 	{
@@ -470,14 +467,13 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 
 // Relax window vertex v of field F (buffers d -> d^1) and, if v is in the
 // check ring (v < chk_e), apply relative_error + is_ok
-// (src/cuda/geodesics_ptp.cu:284-299, 371-375) in FP64.  Returns 1 if v fails
+// (src/cuda/geodesics_ptp.cu:284-299, 371-375).  Returns 1 if v fails
 // the test.  COH: distances may have been written by other CTAs of this launch.
 template <typename T, bool CL, bool COH>
 __device__ __forceinline__ int sweep_vertex(const FieldDev &F, uint32_t d, uint32_t v, uint32_t chk_e)
 {
 	const uint32_t *Co = CL ? F.C[d] : nullptr;
 	uint32_t lab = 0;
-	double o, nd;
 	if constexpr(sizeof(T) == 4)
 	{
 		const float2 *Do = static_cast<const float2 *>(F.D[d]);
@@ -485,8 +481,12 @@ __device__ __forceinline__ int sweep_vertex(const FieldDev &F, uint32_t d, uint3
 		static_cast<float2 *>(F.D[d ^ 1u])[v] = nv;
 		if(v >= chk_e) goto labels;
 		const float2 ov = ld2<COH>(Do + v);
-		o = (double) ov.x + (double) ov.y;
-		nd = (double) nv.x + (double) nv.y;
+		if(CL) F.C[d ^ 1u][v] = lab;
+		// relative_error + is_ok without the division and in FP32: the change
+		// is formed from the hi and lo differences; 0 and INF old values fail
+		// as |new - old| / old does (NaN or INF is not < tol).
+		const float df = (nv.x - ov.x) + (nv.y - ov.y);
+		return !(fabsf(df) < F.tol32 * ov.x);
 	}
 	else
 	{
@@ -494,12 +494,11 @@ __device__ __forceinline__ int sweep_vertex(const FieldDev &F, uint32_t d, uint3
 		const double nv = relax64<CL, COH>(F, v, Do, Co, lab);
 		static_cast<double *>(F.D[d ^ 1u])[v] = nv;
 		if(v >= chk_e) goto labels;
-		o = ld_d<double, COH>(Do + v);
-		nd = nv;
+		const double o = ld_d<double, COH>(Do + v);
+		if(CL) F.C[d ^ 1u][v] = lab;
+		// relative_error + is_ok (src/cuda/geodesics_ptp.cu:284-299, 371-375), in FP64
+		return !(fabs(nv - o) / o < F.tol);
 	}
-	if(CL) F.C[d ^ 1u][v] = lab;
-	// relative_error + is_ok (src/cuda/geodesics_ptp.cu:284-299, 371-375), in FP64
-	return !(fabs(nd - o) / o < F.tol);
 labels:
 	if(CL) F.C[d ^ 1u][v] = lab;
 	return 0;
@@ -1413,11 +1412,11 @@ __global__ void fill_kernel(CatArgs c)
 				// FP32 path only (the FP64 path keeps the reference's triangle order,
 				// so its labels follow the reference's tie rule bit for bit):
 				// start a closed star one before its lowest-numbered neighbour, the
-				// one nearest the sources in ring order.  The two triangles around
-				// it, usually the upwind ones, come first; the downwind ones after
-				// them are then skipped by the triangle pruning in step across the
-				// warp.  The distances do not depend on the order except through
-				// exact ties of rounded candidates.
+				// one nearest the sources in ring order, so the two triangles around
+				// it, usually the upwind ones, come first.  The distances do not
+				// depend on the order except through exact ties of rounded
+				// candidates; a fixed rule keeps the labels of those ties the same
+				// with and without the label field.
 				if(sizeof(T) == 4 && n >= 3 && n <= 8 && (o0f & FAN_CLOSED))
 				{
 					uint32_t m = 0;
