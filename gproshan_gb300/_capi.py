@@ -59,7 +59,7 @@ class gp_call_stats(C.Structure):
                 ("reserved", C.c_uint32), ("ms_toplesets", C.c_double), ("ms_renumber", C.c_double),
                 ("ms_local", C.c_double), ("ms_grid", C.c_double), ("ms_gather", C.c_double),
                 ("relax_local", C.c_uint64), ("relax_grid", C.c_uint64), ("h2d_bytes", C.c_uint64),
-                ("d2h_bytes", C.c_uint64)]
+                ("d2h_bytes", C.c_uint64), ("skip_grid", C.c_uint64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -381,8 +381,10 @@ def ptp(mesh: DeviceMesh, sources, limits=None, sorted_=None, dtype=np.float32, 
 def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP_F32, ctas: int = 0,
               with_stats: bool = True, local_window: int = 0, round_coords: bool = False,
               schedule: int = GP_SCHED_REACTIVE, grid_kernel: int = GP_GRID_AUTO, queue_min: int = 0,
-              queue_tile: int = 0):
-    """Solve many fields together (host arrays).  Returns (dists, stats, seconds)."""
+              queue_tile: int = 0, clusters=None):
+    """Solve many fields together (host arrays).  Returns (dists, stats, seconds).
+    ``clusters``: optional list of per-field uint32 label arrays (initial labels
+    in, labels out, updated in place)."""
     n = len(sources_list)
     out_t = GP_F64 if np.dtype(dtype) == np.float64 else GP_F32
     fields = (gp_field * n)()
@@ -399,6 +401,11 @@ def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP
         fields[k].n_sources = len(src)
         fields[k].dist = d.ctypes.data
         fields[k].clusters = None
+        if clusters is not None and clusters[k] is not None:
+            lab = clusters[k]
+            if lab.dtype != np.uint32 or not lab.flags.c_contiguous or len(lab) != meshes[k].n_vertices:
+                raise ValueError("clusters[k] must be a contiguous uint32 array of n_vertices labels")
+            fields[k].clusters = lab.ctypes.data
         fields[k].stats = C.addressof(stats[k]) if with_stats else None
     sec = C.c_double(0)
     opts = make_opts(precision, ctas=ctas, local_window=local_window, round_coords=round_coords,

@@ -635,11 +635,12 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			}
 			else cs.relax_local += hs[f].relax;
 		}
-		uint32_t hbar[4] = {0, 0, 0, 0};
+		uint32_t hbar[6] = {0, 0, 0, 0, 0, 0};
 		if(stage == Stage::ptp)
 			GP_CUDA(ctx, cudaMemcpy(hbar, P(o_bar), sizeof(hbar), cudaMemcpyDeviceToHost));
 		cs.grid_kernel = hctl.mode;
 		cs.sweeps_grid = hctl.mode == GRID_QUEUE ? hctl.progress : hbar[3];
+		cs.skip_grid = hctl.mode == GRID_QUEUE ? 0 : hbar[4] | (uint64_t) hbar[5] << 32;
 		cs.h2d_bytes = h2d;
 		cs.d2h_bytes = d2h + (stage == Stage::ptp ? 2 * sizeof(hbar) + sizeof(hctl) : 0);
 		ctx->last = cs;

@@ -318,6 +318,22 @@ __device__ __forceinline__ float2 ld2(const float2 *p)
 	else return *p;
 }
 
+// Change flag: distances are >= 0, so the sign bit of a stored hi word is free
+// and marks a value that differs (bitwise) from the one the same sweep read.
+// Buffers start with the flag set on every vertex but the sources (a vertex
+// never relaxed counts as changed).  A window vertex whose own value and every
+// neighbour's value are unflagged, with no neighbour below the window, was
+// relaxed in the previous sweep on exactly the inputs it would read now: its
+// new value is the value it holds, and the solves are skipped (the value is
+// stored again, unflagged).  The neighbours below the window are excluded
+// because they are no longer rewritten, so their two buffers can differ while
+// their flags are stale.  The flags cost one more memory trip, so they are
+// read only by warps whose own 32 values are all unflagged, and only in steps
+// with at least one tile per warp of the launch: a lighter step is bound by
+// the latency of its slowest tile, and the skip would only lengthen it.
+__device__ __forceinline__ float2 unflag(float2 d) { return make_float2(fabsf(d.x), d.y); }
+__device__ __forceinline__ bool flagged(float h) { return (__float_as_uint(h) >> 31) != 0u; }
+
 // (t, residual): t = (dv - base) rounded, t + residual the exact difference
 // up to the lo parts' own rounding.  The hi difference is formed exactly too
 // (TwoSum): a neighbour much nearer or farther than the base (a long edge next
@@ -386,19 +402,19 @@ __device__ __noinline__ float2 relax32_csr(const FieldDev &F, uint32_t v, const 
 	if(bh == INFINITY)
 	{
 		float m = INFINITY;
-		for(uint32_t k = 0; k < n; k++) m = fminf(m, ld2<COH>(Do + __ldg(fan + k)).x);
+		for(uint32_t k = 0; k < n; k++) m = fminf(m, fabsf(ld2<COH>(Do + __ldg(fan + k)).x));
 		bh = m == INFINITY ? 0.f : m;
 		bl = 0.f;
 	}
 	const float old_rel = vd.x == INFINITY ? INFINITY : 0.f;
 	Cand32 best = {old_rel, 0.f, 0.f, 0.f};
 	const uint32_t w0 = __ldg(fan);
-	const Nb32 first = make_nb(__ldg(F.P + w0), rel_to(ld2<COH>(Do + w0), bh, bl), pv, w0);
+	const Nb32 first = make_nb(__ldg(F.P + w0), rel_to(unflag(ld2<COH>(Do + w0)), bh, bl), pv, w0);
 	Nb32 last = first;
 	for(uint32_t e = 1; e < n; e++)
 	{
 		const uint32_t w = __ldg(fan + e);
-		const Nb32 cur = make_nb(__ldg(F.P + w), rel_to(ld2<COH>(Do + w), bh, bl), pv, w);
+		const Nb32 cur = make_nb(__ldg(F.P + w), rel_to(unflag(ld2<COH>(Do + w)), bh, bl), pv, w);
 		take32<CL, COH>(last, cur, best, lab, Co);
 		last = cur;
 	}
@@ -409,11 +425,12 @@ __device__ __noinline__ float2 relax32_csr(const FieldDev &F, uint32_t v, const 
 
 template <bool CL, bool COH>
 __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const float2 *Do, const uint32_t *Co,
-                                          uint32_t &lab)
+                                          uint32_t &lab, uint32_t win_s, bool try_skip, float2 &vd, bool &skip)
 {
 	// the fan row, the vertex's own distance and position: one memory trip
 	const uint4 ra = __ldg(F.fan8 + 2 * (size_t) v), rb = __ldg(F.fan8 + 2 * (size_t) v + 1);
-	const float2 vd = ld2<COH>(Do + v);
+	const float2 vs = ld2<COH>(Do + v);
+	vd = unflag(vs);
 	const float4 pv = __ldg(F.P + v);
 	if(CL) lab = ld_d<uint32_t, COH>(Co + v);
 	uint32_t u[FB] = {ra.x & FAN_MASK, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
@@ -423,6 +440,24 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 #pragma unroll
 	for(uint32_t k = 0; k < FB; k++) n += (k == 0 ? ra.x : u[k]) != FAN8_EMPTY;
 	if(!n) return vd;
+	// inputs unchanged since the previous sweep: the value stands (labels
+	// always take the full path: a tie can move a label without a distance)
+	if(!CL && try_skip)
+	{
+		const unsigned am = __activemask();
+		if(__all_sync(am, !flagged(vs.x)))
+		{
+			bool same = true;
+#pragma unroll
+			for(uint32_t k = 0; k < FB; k++)
+				if(k < n) same &= u[k] >= win_s && !flagged(ld_d<float, COH>(reinterpret_cast<const float *>(Do + u[k])));
+			if(same)
+			{
+				skip = true;
+				return vd;
+			}
+		}
+	}
 	// base of the relative distances: the vertex itself, or (while it is INF)
 	// its smallest neighbour
 	float bh = vd.x, bl = vd.y;
@@ -431,7 +466,7 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 		float m = INFINITY;
 #pragma unroll
 		for(uint32_t k = 0; k < FB; k++)
-			if(k < n) m = fminf(m, ld2<COH>(Do + u[k]).x);
+			if(k < n) m = fminf(m, fabsf(ld2<COH>(Do + u[k]).x));
 		bh = m == INFINITY ? 0.f : m;
 		bl = 0.f;
 	}
@@ -454,7 +489,7 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 		for(uint32_t q = 0; q < FC; q++)
 			if(c + q < n)
 			{
-				const Nb32 cur = make_nb(pk[q], rel_to(dk[q], bh, bl), pv, u[c + q]);
+				const Nb32 cur = make_nb(pk[q], rel_to(unflag(dk[q]), bh, bl), pv, u[c + q]);
 				if(c + q == 0) first = cur;
 				else take32<CL, COH>(last, cur, best, lab, Co);
 				last = cur;
@@ -470,17 +505,21 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 // (src/cuda/geodesics_ptp.cu:284-299, 371-375).  Returns 1 if v fails
 // the test.  COH: distances may have been written by other CTAs of this launch.
 template <typename T, bool CL, bool COH>
-__device__ __forceinline__ int sweep_vertex(const FieldDev &F, uint32_t d, uint32_t v, uint32_t chk_e)
+__device__ __forceinline__ int sweep_vertex(const FieldDev &F, uint32_t d, uint32_t v, uint32_t win_s, uint32_t chk_e,
+                                            bool try_skip = false, bool *skipped = nullptr)
 {
 	const uint32_t *Co = CL ? F.C[d] : nullptr;
 	uint32_t lab = 0;
 	if constexpr(sizeof(T) == 4)
 	{
 		const float2 *Do = static_cast<const float2 *>(F.D[d]);
-		const float2 nv = relax32<CL, COH>(F, v, Do, Co, lab);
-		static_cast<float2 *>(F.D[d ^ 1u])[v] = nv;
+		float2 ov;
+		bool skip = false;
+		const float2 nv = relax32<CL, COH>(F, v, Do, Co, lab, win_s, try_skip, ov, skip);
+		if(skipped) *skipped = skip;
+		const bool chg = __float_as_uint(nv.x) != __float_as_uint(ov.x) || __float_as_uint(nv.y) != __float_as_uint(ov.y);
+		static_cast<float2 *>(F.D[d ^ 1u])[v] = make_float2(__uint_as_float(__float_as_uint(nv.x) | (chg ? 0x80000000u : 0u)), nv.y);
 		if(v >= chk_e) goto labels;
-		const float2 ov = ld2<COH>(Do + v);
 		if(CL) F.C[d ^ 1u][v] = lab;
 		// relative_error + is_ok without the division and in FP32: the change
 		// is formed from the hi and lo differences; 0 and INF old values fail
@@ -662,7 +701,7 @@ __global__ void __launch_bounds__(LT) ptp_local_kernel(FieldDev *fields, FieldSt
 		{
 			int bad = 0;
 			for(uint32_t v = st.win_s + threadIdx.x; v < st.win_e; v += LT)
-				bad |= sweep_vertex<T, CL, false>(F, st.d, v, st.chk_e);
+				bad |= sweep_vertex<T, CL, false>(F, st.d, v, st.win_s, st.chk_e);
 			close_sweep(st, !__syncthreads_or(bad));
 			open_sweep(F, st, threadIdx.x == 0);
 		}
@@ -885,6 +924,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	}
 	const uint32_t G = s_G;
 	__shared__ uint32_t s_tile;  // the CTA's next tile (see the step loop)
+	uint32_t n_skip = 0;  // this thread's relaxations skipped as unchanged (summed into bar[4..5] at the end)
 	grid_plan<TV>(fs, ts, G, &s_tile);
 	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
 
@@ -901,9 +941,12 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		if(!total)
 		{
 			if(blockIdx.x == 0 && threadIdx.x == 0) a.bar[3] = step;
+			const uint32_t w = __reduce_add_sync(0xffffffffu, n_skip);
+			if(lane == 0 && w) atomicAdd(reinterpret_cast<unsigned long long *>(a.bar + 4), (unsigned long long) w);
 			break;
 		}
 		uint32_t *flags = a.notok + (step % 3) * F;
+		const bool heavy = total >= gridDim.x * (NT / 32);  // see unflag: skip only in throughput-bound steps
 		uint32_t lo = 0;  // entry of the warp's current tile; tiles only move forward
 		// CTA b (one per SM) owns tiles b, b + C, b + 2C, ...; its 32 warps take
 		// them in order from a shared counter (reset by grid_plan), so they all
@@ -929,8 +972,10 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			const SchedSmem &x = fs[lo];
 			const uint32_t f = id[lo];
 			int bad = 0;
+			bool sk = false;
 			const uint32_t v = x.win_s + (k - ts[lo]) * TV + lane;
-			if(v < x.win_e) bad = sweep_vertex<T, CL, true>(a.fields[f], x.d, v, x.chk_e);
+			if(v < x.win_e) bad = sweep_vertex<T, CL, true>(a.fields[f], x.d, v, x.win_s, x.chk_e, heavy, &sk);
+			n_skip += sk;
 			// one atomic per warp that saw a failure, no block barrier per tile
 			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
 		}
@@ -1268,7 +1313,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_queue_kernel(QueueArgs a
 		for(uint32_t g = 0; g < groups; g++)
 		{
 			const uint32_t v = win_s + (tile * groups + g) * 32u + lane;
-			if(v < win_e) bad |= sweep_vertex<T, CL, true>(F, d, v, chk_e);
+			if(v < win_e) bad |= sweep_vertex<T, CL, true>(F, d, v, win_s, chk_e);
 		}
 		if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(&a.qf[q].notok[e & 1u], 1u);
 		__syncwarp();
@@ -1440,7 +1485,8 @@ __global__ void fill_kernel(CatArgs c)
 				F.Pd[4 * (size_t) k + 3] = 0.0;
 			}
 			S d0;
-			if constexpr(sizeof(T) == 4) d0 = make_float2(k < n0 ? 0.f : INFINITY, 0.f);
+			// FP32: every vertex but the sources starts flagged as changed
+			if constexpr(sizeof(T) == 4) d0 = make_float2(k < n0 ? 0.f : -INFINITY, 0.f);
 			else d0 = k < n0 ? 0.0 : (double) INFINITY;
 			D0[k] = d0;
 			D1[k] = d0;
@@ -1492,7 +1538,7 @@ __global__ void gather_kernel(CatArgs c)
 		double x;
 		if constexpr(sizeof(T) == 4)
 		{
-			const float2 h = static_cast<const float2 *>(F.D[st.d])[k];
+			const float2 h = unflag(static_cast<const float2 *>(F.D[st.d])[k]);
 			x = (double) h.x + (double) h.y;
 		}
 		else x = static_cast<const double *>(F.D[st.d])[k];

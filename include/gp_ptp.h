@@ -209,6 +209,8 @@ typedef struct gp_call_stats {
 	uint64_t relax_grid;       /* vertex relaxations done by the grid-wide launch */
 	uint64_t h2d_bytes;        /* host -> device bytes copied by the call */
 	uint64_t d2h_bytes;        /* device -> host bytes copied by the call */
+	uint64_t skip_grid;        /* relaxations of the lockstep launch whose inputs were unchanged since the
+	                              previous sweep (FP32 without labels): solves skipped, same result */
 } gp_call_stats;
 
 gp_status gp_ctx_call_stats(const gp_ctx *ctx, gp_call_stats *out);

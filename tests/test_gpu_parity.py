@@ -332,6 +332,60 @@ def test_queue_and_lockstep_grid_kernels_agree(gpu_ctx, precision, clusters):
         assert np.array_equal(d, b[0][k]) and st.n_iter == b[2][k][0], k
 
 
+@pytest.mark.parametrize("launch", ["cta", "lockstep", "queue"])
+def test_change_flags_leave_distances_unchanged(gpu_ctx, launch):
+    """The FP32 sweeps without labels keep a change flag in the sign bit of
+    every stored distance; the labelled sweeps run the same arithmetic.  Both
+    give the same distance bits and sweep counts on every launch kind."""
+    from gproshan_gb300 import _capi, meshgen
+    kw = {"cta": dict(local_window=1 << 30), "lockstep": dict(local_window=1, grid_kernel=_capi.GP_GRID_LOCKSTEP),
+          "queue": dict(local_window=1, grid_kernel=_capi.GP_GRID_QUEUE, queue_min=1)}[launch]
+    cases = [(meshgen.height_field(150, 3), [7]), (meshgen.torus(60, 300, seed=2), [0, 9000])]
+    for (xyz, tri), src in cases:
+        m = dev_mesh(gpu_ctx, xyz, tri)
+        a, _, sa = _capi.ptp(m, src, opts=_capi.make_opts(0, **kw))
+        b, _, sb = _capi.ptp(m, src, clusters=np.zeros(len(xyz), np.uint32), opts=_capi.make_opts(0, **kw))
+        assert sa.n_iter == sb.n_iter and sa.relaxations == sb.relaxations
+        assert np.array_equal(a, b), np.max(np.abs(a.astype(np.float64) - b))
+        assert np.all(a >= 0)  # no flag leaks into the output
+
+
+def test_unchanged_input_skip_is_exact(gpu_ctx, oracle_lib):
+    """In steps of the lockstep launch with at least one tile per warp, a warp
+    whose vertices and their neighbours did not change in the previous sweep
+    skips the solves.  The skip happens (counted) and changes nothing: the
+    distances equal the labelled run's (which never skips) bit for bit, and a
+    sample matches the FP64 oracle within the FP32 bar."""
+    from gproshan_gb300 import _capi, meshgen
+    meshes = [meshgen.height_field(256, 11), meshgen.torus(60, 300, seed=2)]
+    dms = [dev_mesh(gpu_ctx, x, t) for x, t in meshes]
+    rng = np.random.default_rng(5)
+    ms, srcs, mi = [], [], []
+    for k in range(40):
+        q = k % 2
+        ms.append(dms[q])
+        mi.append(q)
+        srcs.append(rng.choice(dms[q].n_vertices, size=1 + k % 2, replace=False))
+    kw = dict(local_window=1, grid_kernel=_capi.GP_GRID_LOCKSTEP)
+    a, sa, _ = _capi.ptp_batch(gpu_ctx, ms, srcs, **kw)
+    cs = gpu_ctx.call_stats()
+    assert cs.grid_kernel == _capi.GP_GRID_LOCKSTEP and cs.fields_grid == len(ms)
+    assert cs.skip_grid > 0.02 * cs.relax_grid, (cs.skip_grid, cs.relax_grid)
+    labs = [np.zeros(m.n_vertices, np.uint32) for m in ms]
+    b, sb, _ = _capi.ptp_batch(gpu_ctx, ms, srcs, clusters=labs, **kw)
+    assert gpu_ctx.call_stats().skip_grid == 0
+    for k in range(len(ms)):
+        assert sa[k].n_iter == sb[k].n_iter, k
+        assert np.array_equal(a[k], b[k]), k
+    for k in (0, 1, 6):
+        x, t = meshes[mi[k]]
+        om = oracle_lib.Mesh(x, t)
+        _, s_o, l_o = oracle_lib.toplesets(om, srcs[k])
+        ref = oracle_lib.ptp(om, srcs[k], l_o, s_o, xyz=x.astype(np.float32).astype(np.float64))
+        assert sa[k].n_iter == ref["n_iter"]
+        assert oracle_lib.max_rel_err(a[k], ref["dist"]) <= REL_TOL_F32
+
+
 def test_queue_kernel_auto_choice(gpu_ctx):
     """GP_GRID_AUTO takes the lockstep launch below queue_min grid fields and
     the work queue from there on."""
