@@ -51,27 +51,46 @@ __device__ __forceinline__ uint32_t slot_of(const uint4 &a, const uint4 &b, uint
 // smaller key (its discoverer sat at an earlier position), and the sources
 // hold key 0 (set when seeded), so the min leaves them unchanged; a key match
 // at emit time therefore means "unvisited and first met here".
-__device__ __forceinline__ void discover(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &ra, const uint4 &rb)
+// The keys are read first and the atomic is issued only where the key read is
+// larger than ours (keys only decrease, so a smaller one stays smaller): on a
+// mesh about two thirds of a frontier vertex's links lead back to visited
+// vertices, and a level's atomics, all issued by one SM, dominated its time.
+// Returns the slots that were not already smaller (the only slots this
+// position can own); overflow rows return every slot.
+__device__ __forceinline__ uint32_t discover(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &ra, const uint4 &rb)
 {
 	if(rb.w == FAN8_OVERFLOW)
 	{
 		const uint32_t o0 = __ldg(F.m.fan_off + v) & FAN_MASK, o1 = __ldg(F.m.fan_off + v + 1) & FAN_MASK;
 		for(uint32_t e = o0; e < o1; e++)
 			atomicMin(F.key + __ldg(F.m.fan + e), (((unsigned long long) p << 20) | (e - o0)) + 1);
-		return;
+		return 0xFFu;
 	}
+	unsigned long long k[8];
 #pragma unroll
 	for(uint32_t q = 0; q < 8; q++)
 	{
 		const uint32_t u = slot_of(ra, rb, q);
-		if(u != FAN8_EMPTY) atomicMin(F.key + u, (((unsigned long long) p << 20) | q) + 1);
+		k[q] = u != FAN8_EMPTY ? ldcg(F.key + u) : 0ull;
 	}
+	uint32_t cand = 0;
+#pragma unroll
+	for(uint32_t q = 0; q < 8; q++)
+	{
+		const unsigned long long mine = (((unsigned long long) p << 20) | q) + 1;
+		if(k[q] > mine)
+		{
+			atomicMin(F.key + slot_of(ra, rb, q), mine);
+			cand |= 1u << q;
+		}
+	}
+	return cand;
 }
 
 // The vertices owned by frontier position p (key match), as a slot mask;
 // overflow rows report their count and are re-walked at emit time.
 __device__ __forceinline__ uint32_t owned(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &ra, const uint4 &rb,
-                                          uint32_t &count)
+                                          uint32_t &count, uint32_t cand = 0xFFu)
 {
 	uint32_t mask = 0;
 	count = 0;
@@ -86,7 +105,8 @@ __device__ __forceinline__ uint32_t owned(const FieldDev &F, uint32_t p, uint32_
 	for(uint32_t q = 0; q < 8; q++)
 	{
 		const uint32_t u = slot_of(ra, rb, q);
-		if(u != FAN8_EMPTY && ldcg(F.key + u) == (((unsigned long long) p << 20) | q) + 1) mask |= 1u << q;
+		if((cand >> q & 1u) && u != FAN8_EMPTY && ldcg(F.key + u) == (((unsigned long long) p << 20) | q) + 1)
+			mask |= 1u << q;
 	}
 	count = __popc(mask);
 	return mask;
@@ -114,7 +134,7 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 		{
 			// pass 1: rows of the frontier (first KB chunks kept in registers), discover
 			uint4 ra[KB], rb[KB];
-			uint32_t vv[KB];
+			uint32_t vv[KB], cm[KB];
 #pragma unroll
 			for(uint32_t c = 0; c < KB; c++)
 			{
@@ -124,7 +144,7 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 					vv[c] = in_smem ? sf[cur][p - s] : ldcg(F.sorted + p);
 					ra[c] = __ldg(F.m.fan8 + 2 * (size_t) vv[c]);
 					rb[c] = __ldg(F.m.fan8 + 2 * (size_t) vv[c] + 1);
-					discover(F, p, vv[c], ra[c], rb[c]);
+					cm[c] = discover(F, p, vv[c], ra[c], rb[c]);
 				}
 			}
 			for(uint32_t p = s + SF + threadIdx.x; p < e; p += BT)
@@ -138,7 +158,7 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 			for(uint32_t base = s, c = 0; base < e; base += BT, c++)
 			{
 				const uint32_t p = base + threadIdx.x;
-				uint32_t v = 0, cnt = 0, mask = 0;
+				uint32_t v = 0, cnt = 0, mask = 0, cand = 0xFFu;
 				uint4 a = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY), b = a;
 				if(p < e)
 				{
@@ -152,6 +172,7 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 								v = vv[k];
 								a = ra[k];
 								b = rb[k];
+								cand = cm[k];
 							}
 					}
 					else
@@ -160,7 +181,7 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 						a = __ldg(F.m.fan8 + 2 * (size_t) v);
 						b = __ldg(F.m.fan8 + 2 * (size_t) v + 1);
 					}
-					mask = owned(F, p, v, a, b, cnt);
+					mask = owned(F, p, v, a, b, cnt, cand);
 				}
 				uint32_t tot;
 				const uint32_t ex = block_exclusive_scan<BT>(cnt, &tot);
