@@ -197,6 +197,8 @@ enum class Stage { toplesets, features, ptp };
 
 // GP_GRID_AUTO takes the work queue from this many grid fields on
 constexpr uint32_t QUEUE_MIN_DEFAULT = 0xFFFFFFFFu;
+// Default window above which a field leaves the one-CTA launch, per precision.
+constexpr uint32_t LOCAL_WINDOW_F32 = 4096u, LOCAL_WINDOW_F64 = 256u;
 
 // Toplesets of a call with at most WIDE_MAX_FIELDS fields run every field on
 // a mesh of at least WIDE_MIN_VERTICES vertices on the whole GPU (one level
@@ -517,7 +519,10 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		                                   reinterpret_cast<uint32_t *>(P(o_scan)), f64, clusters, s));
 		cs.launches += 4 + scan_launches(tot);
 		GP_CUDA(ctx, record(ctx->ph[2]));
-		const uint32_t lw = o.local_window ? o.local_window : 4096u;
+		// FP64 fields leave the one-CTA launch early: GB300's FP64 pipe retires
+		// ~2 FMAs per clock per SM, so one CTA is throughput-bound on one SM
+		// (icosphere L6: 37.8 ms at 4096, 8.9 ms at <= 256)
+		const uint32_t lw = o.local_window ? o.local_window : (f64 ? LOCAL_WINDOW_F64 : LOCAL_WINDOW_F32);
 		uint32_t *pbig = nullptr, *perm = nullptr;
 		if(learned)
 		{
@@ -1172,7 +1177,10 @@ gp_status gp_ptp_autotune(gp_ctx *ctx, const gp_field *fields, uint32_t n_fields
 	gp_ptp_opts cur = *opts, best_o = *opts;
 	double best = INFINITY, t = 0;
 	cur.grid_kernel = GP_GRID_LOCKSTEP;
-	for(uint32_t lw : {1024u, 2048u, 4096u, 8192u, 16384u})
+	const bool f64 = opts->precision == GP_F64;
+	const std::initializer_list<uint32_t> windows32 = {1024u, 2048u, 4096u, 8192u, 16384u};
+	const std::initializer_list<uint32_t> windows64 = {64u, 256u, 1024u, 4096u};
+	for(uint32_t lw : f64 ? windows64 : windows32)
 	{
 		cur.local_window = lw;
 		const gp_status st = timed(cur, t);

@@ -34,7 +34,7 @@ constexpr int BT = GP_BT;  // threads of a BFS CTA
 // Frontier vertices whose link rows a thread keeps in registers between the
 // two passes of a level, and the shared-memory copy of the frontier.
 #ifndef GP_KB
-#define GP_KB 2
+#define GP_KB 1
 #endif
 constexpr uint32_t KB = GP_KB;
 constexpr uint32_t SF = BT * KB;

@@ -111,7 +111,7 @@ typedef struct gp_ptp_opts {
 	uint32_t threads;      /* reserved (threads per CTA are fixed per kernel) */
 	uint32_t ctas;         /* CTAs of the grid-wide launch, 0: all that fit */
 	uint32_t local_window; /* fields whose windows stay within this many vertices are
-	                          swept by one CTA each; 0: default (4096) */
+	                          swept by one CTA each; 0: default (GP_F32: 4096, GP_F64: 256) */
 	uint32_t round_coords; /* GP_F64 only: 1 = solve on the float-rounded coordinates
 	                          the GP_F32 path sees (an FP64 check of an FP32 run) */
 	uint32_t schedule;     /* GP_SCHED_REACTIVE (0) or GP_SCHED_LEARNED (1): see below */
