@@ -46,8 +46,7 @@ struct GridSync {
 constexpr uint32_t QUEUE_STRIPES = 4;
 // words of the lockstep grid launch's barrier block: [0] top arrivals, [1]
 // abort, [2] error bits, [3] steps, then 16 group counters on 128-byte lines
-constexpr uint32_t GRID_BAR_GROUPS = 16;
-constexpr uint32_t GRID_BAR_WORDS = 32 * (GRID_BAR_GROUPS + 1);
+constexpr uint32_t GRID_BAR_WORDS = 32;  // one 128-byte line: see count_barrier
 constexpr uint32_t GRID_NONE = 0, GRID_LOCKSTEP = 1, GRID_QUEUE = 2;
 
 struct alignas(128) QLine {

@@ -793,13 +793,13 @@ __device__ __forceinline__ void open_sweep_cached(const FieldDev *F, FieldState 
 	else st.live = 0;
 }
 
-// Counting barrier in two levels: a CTA arrives on its group's counter
-// (acquire-release add; GRID_BAR_GROUPS groups, one 128-byte line each, so the
-// arrivals are spread over several L2 slices), the last CTA of a group
-// arrives on the top counter (release add), and every CTA waits for all
-// groups with an acquire spin.  Bounded: gives up after `limit` polls (error
-// bit set, abort raised, caller returns).  bar: [0] top arrivals, [1] abort,
-// [2] error bits, [3] steps; group g counts at bar[32 * (g + 1)].
+// Counting barrier: every CTA arrives with a fire-and-forget release add on
+// one counter and waits with an acquire spin until all CTAs of the step have
+// arrived.  (A two-level form, CTAs counted on 16 group counters whose last
+// arrival then signals the top counter, needs a returning atomic per CTA:
+// one more L2 round trip per step, measured 2-13 % slower.)  Bounded: gives
+// up after `limit` polls (error bit set, abort raised, caller returns).
+// bar: [0] arrivals, [1] abort, [2] error bits, [3] steps, [4..5] skip count.
 
 __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint32_t limit, uint32_t phantom)
 {
@@ -808,12 +808,8 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint
 	if(threadIdx.x == 0)
 	{
 		s_ok = 1;
-		const uint32_t groups = min(GRID_BAR_GROUPS, gridDim.x), g = blockIdx.x % groups;
-		const uint32_t members = gridDim.x / groups + (g < gridDim.x % groups ? 1u : 0u);
-		const uint32_t old = atom_add_acq_rel(bar + 32 * (g + 1), 1u);
-		if(old + 1 == members * (step + 1))
-			asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
-		const uint32_t target = (groups + phantom) * (step + 1);
+		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
+		const uint32_t target = (gridDim.x + phantom) * (step + 1);
 		uint32_t spins = 0;
 		while(ld_acquire(bar) < target)
 		{
