@@ -1429,12 +1429,6 @@ __global__ void fill_kernel(CatArgs c)
 			const uint32_t o0f = F.m.fan_off[v];
 			const uint32_t o0 = o0f & FAN_MASK, o1 = F.m.fan_off[v + 1] & FAN_MASK;
 			const uint32_t dst = c.cnt[g];
-			for(uint32_t e = o0; e < o1; e++)
-			{
-				const uint32_t u = F.m.fan[e];
-				const uint32_t iu = F.inv[u];
-				F.fan[dst + (e - o0)] = iu ? iu - 1 : nr;
-			}
 			F.off[k] = dst | (o0f & FAN_CLOSED);
 			{
 				uint32_t r[8];
@@ -1449,6 +1443,20 @@ __global__ void fill_kernel(CatArgs c)
 					}
 					r[q] = x;
 				}
+				// the renumbered CSR fan: read by the FP64 sweeps, and by the FP32
+				// sweeps only for rows of more than 8 entries
+				if(sizeof(T) == 8 || n > 8)
+					for(uint32_t e = o0; e < o1; e++)
+					{
+						const uint32_t q = e - o0;
+						uint32_t x = q < 8 ? r[q] : 0u;
+						if(q >= 8)
+						{
+							const uint32_t iu = F.inv[F.m.fan[e]];
+							x = iu ? iu - 1 : nr;
+						}
+						F.fan[dst + q] = x;
+					}
 				if(n > 8) r[7] = FAN8_OVERFLOW;
 				// FP32 path only (the FP64 path keeps the reference's triangle order,
 				// so its labels follow the reference's tie rule bit for bit):
