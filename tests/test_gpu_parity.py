@@ -455,3 +455,22 @@ def test_toplesets_high_valence_vertex(gpu_ctx, oracle_lib):
         ref32 = oracle_lib.ptp(om, src, l_o, s_o, xyz=xyz.astype(np.float32).astype(np.float64))
         d32, _, _ = _capi.ptp(m, src)
         assert oracle_lib.max_rel_err(d32, ref32["dist"]) <= REL_TOL_F32
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["flat101", "sphere_L5"])
+def test_accuracy_against_closed_form_matches_oracle(gpu_ctx, oracle_lib, case):
+    """Against exact geodesics (flat grid: Euclidean; unit sphere:
+    great-circle), the FP32 GPU path has the algorithm's own error profile:
+    the mean relative error the reference's harness reports equals the FP64
+    oracle's to within 1e-3 percentage points."""
+    from gproshan_gb300 import _capi
+    from test_oracle import _closed_form_cases, mean_rel_err_pct
+    name, xyz, tri, src, exact = _closed_form_cases()[case]
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    d, _, st = _capi.ptp(m, [src])
+    om = oracle_lib.Mesh(xyz, tri)
+    ref = oracle_lib.ptp(om, [src], xyz=xyz.astype(np.float32).astype(np.float64))
+    assert st.n_iter == ref["n_iter"]
+    e_gpu = mean_rel_err_pct(d.astype(np.float64), exact)
+    e_ref = mean_rel_err_pct(ref["dist"], exact)
+    assert abs(e_gpu - e_ref) < 1e-3, (name, e_gpu, e_ref)

@@ -99,3 +99,36 @@ def test_oracle_vs_reference_random_meshes(oracle_lib):
         assert np.array_equal(r1, r2) and np.array_equal(s1, s2) and np.array_equal(l1, l2)
         out = oracle_lib.ptp(m, src, l1, s1)
         assert np.array_equal(out["dist_cpu"], rm.ptp_cpu(src, l2, s2))
+
+
+def _closed_form_cases():
+    """A flat grid (exact geodesic = Euclidean distance) and a unit icosphere
+    (exact = great-circle angle), with their sources."""
+    from gproshan_gb300 import meshgen
+    flat, ft = meshgen.height_field(101, 0)
+    flat = flat.copy()
+    flat[:, 2] = 0.0
+    fs = 50 * 101 + 50
+    sph, st = meshgen.icosphere(5, 0.0, 0)
+    sph = sph / np.linalg.norm(sph, axis=1)[:, None]
+    return [("flat101", flat, ft, fs, np.linalg.norm(flat - flat[fs], axis=1)),
+            ("sphere_L5", sph, st, 0, np.arccos(np.clip(sph @ sph[0], -1.0, 1.0)))]
+
+
+def mean_rel_err_pct(dist, exact):
+    """compute_error of the reference's harness (src/test_geodesics_ptp.cpp:362-371):
+    mean relative error in %, over the vertices whose exact distance is > 0."""
+    m = exact > 0
+    return 100.0 * float(np.mean(np.abs(dist[m] - exact[m]) / exact[m]))
+
+
+@pytest.mark.parametrize("case", [0, 1], ids=["flat101", "sphere_L5"])
+def test_accuracy_against_closed_form_geodesics(oracle_lib, case):
+    """The PTP algorithm's own accuracy, the quantity the reference's
+    test_geodesics harness reports against exact distances: ~1.4 % mean
+    relative error on a flat grid, ~1.0 % on a unit sphere."""
+    name, xyz, tri, src, exact = _closed_form_cases()[case]
+    m = oracle_lib.Mesh(xyz, tri)
+    r = oracle_lib.ptp(m, [src])
+    err = mean_rel_err_pct(r["dist"], exact)
+    assert err < {"flat101": 1.5, "sphere_L5": 1.0}[name], (name, err)
