@@ -820,7 +820,8 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint
 		uint32_t spins = 0;
 		while(ld_acquire(bar) < target)
 		{
-			if(++spins > limit || ld_relaxed(bar + 1))
+			// another CTA's abort is looked for every 32 polls (one load per poll)
+			if(++spins > limit || ((spins & 31u) == 0 && ld_relaxed(bar + 1)))
 			{
 				atomicOr(bar + 2, DEV_ERR_TIMEOUT);
 				atomicExch(bar + 1, 1u);
