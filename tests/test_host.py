@@ -110,3 +110,36 @@ def test_cpp_dropin_shim_compiles_against_reference_headers():
                             "-I", os.path.join(ROOT, "oracle", "stubs"), "-I", ref,
                             "-I", os.path.join(ROOT, "include"), shim], capture_output=True, text=True)
         assert r.returncode == 0, r.stderr
+
+
+def test_ctypes_struct_layouts_match_the_header(tmp_path):
+    """Every struct the ctypes binding mirrors has the header's size and field
+    offsets (a C probe compiled against include/gp_ptp.h prints them)."""
+    import shutil
+    import subprocess
+    from gproshan_gb300 import _capi
+    if not shutil.which("gcc"):
+        pytest.skip("no C compiler")
+    structs = [_capi.gp_ptp_opts, _capi.gp_ptp_stats, _capi.gp_call_stats, _capi.gp_field]
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "gp_ptp.h"', 'int main(void) {']
+    for st in structs:
+        name = st.__name__
+        lines.append(f'printf("{name} size %zu\\n", sizeof({name}));')
+        for fname, _ in st._fields_:
+            lines.append(f'printf("{name} {fname} %zu\\n", offsetof({name}, {fname}));')
+    lines += ['return 0;', '}']
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c11", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split("\n")
+    got = {}
+    for line in out:
+        if line:
+            *key, val = line.split()
+            got[tuple(key)] = int(val)
+    for st in structs:
+        name = st.__name__
+        assert got[(name, "size")] == ctypes.sizeof(st), name
+        for fname, _ in st._fields_:
+            assert got[(name, fname)] == getattr(st, fname).offset, (name, fname)
