@@ -474,3 +474,46 @@ def test_accuracy_against_closed_form_matches_oracle(gpu_ctx, oracle_lib, case):
     e_gpu = mean_rel_err_pct(d.astype(np.float64), exact)
     e_ref = mean_rel_err_pct(ref["dist"], exact)
     assert abs(e_gpu - e_ref) < 1e-3, (name, e_gpu, e_ref)
+
+
+def _uv_sphere(n_lon=64, n_lat=48):
+    """Latitude-longitude sphere: two poles of valence n_lon (rows past 8
+    entries, read from the CSR lists) surrounded by needle triangles."""
+    th = np.linspace(0, np.pi, n_lat + 1)[1:-1]
+    ph = np.linspace(0, 2 * np.pi, n_lon, endpoint=False)
+    T, P = np.meshgrid(th, ph, indexing="ij")
+    ring = np.stack([np.sin(T) * np.cos(P), np.sin(T) * np.sin(P), np.cos(T)], -1).reshape(-1, 3)
+    xyz = np.concatenate([[[0.0, 0.0, 1.0]], ring, [[0.0, 0.0, -1.0]]])
+    south = len(xyz) - 1
+    idx = lambda r, c: 1 + r * n_lon + c % n_lon
+    tri = []
+    for c in range(n_lon):
+        tri.append([0, idx(0, c), idx(0, c + 1)])
+        tri.append([south, idx(n_lat - 2, c + 1), idx(n_lat - 2, c)])
+        for r in range(n_lat - 2):
+            a, b, cc, d = idx(r, c), idx(r, c + 1), idx(r + 1, c), idx(r + 1, c + 1)
+            tri += [[a, cc, b], [b, cc, d]]
+    return xyz, np.array(tri, np.uint32)
+
+
+@pytest.mark.parametrize("src", [[0], [1000], [0, 1500]])
+def test_high_valence_poles_on_the_grid_launch(gpu_ctx, oracle_lib, src):
+    """Vertices of valence 64 swept by the grid-wide lockstep launch: FP64
+    bit-exact with the oracle, FP32 within the bar with the same sweeps, and
+    the FP32 distances the same with and without labels."""
+    from gproshan_gb300 import _capi
+    xyz, tri = _uv_sphere()
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    _, s_o, l_o = oracle_lib.toplesets(om, src)
+    kw = dict(local_window=1, grid_kernel=_capi.GP_GRID_LOCKSTEP)
+    ref = oracle_lib.ptp(om, src, l_o, s_o)
+    d64, _, st = _capi.ptp(m, src, dtype=np.float64, opts=_capi.make_opts(_capi.GP_F64, **kw))
+    assert gpu_ctx.call_stats().fields_grid == 1
+    assert st.n_iter == ref["n_iter"] and np.array_equal(d64, ref["dist"])
+    ref32 = oracle_lib.ptp(om, src, l_o, s_o, xyz=xyz.astype(np.float32).astype(np.float64))
+    d32, _, st32 = _capi.ptp(m, src, opts=_capi.make_opts(_capi.GP_F32, **kw))
+    assert st32.n_iter == ref32["n_iter"]
+    assert oracle_lib.max_rel_err(d32, ref32["dist"]) <= REL_TOL_F32
+    d32c, _, _ = _capi.ptp(m, src, clusters=np.zeros(len(xyz), np.uint32), opts=_capi.make_opts(_capi.GP_F32, **kw))
+    assert np.array_equal(d32, d32c)
