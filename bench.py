@@ -460,7 +460,10 @@ def main():
         "warmup": args.warmup, "ms_per_step": res["ms_batched"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": WORKLOAD, "fields": F, "vertices_per_step": res["nv_total"] * world,
-                   "relaxations_per_step": res["relax_total"] * world, "parallelism": f"fields x{world}",
+                   "relaxations_per_step": res["relax_total"] * world,
+                   "relaxations_per_s": res["relax_total"] * world / (res["ms_batched"] * 1e-3)
+                   if res["ms_batched"] else None,
+                   "parallelism": f"fields x{world}",
                    "schedule": args.schedule, "grid_kernel": res["grid_kernel"], "autotuned": res["tuned"],
                    "cuda_graph": res["graph"],
                    "l2": "inputs larger than L2 (129 MB): the step touches every mesh and field buffer"},
