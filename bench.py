@@ -19,12 +19,18 @@ events on the library's stream.
              reference `che` does between calls);
 * roofline -- the sweep launch's algorithmic bytes (48 per relaxation) over
              its CUDA-event time, against the measured HBM copy bandwidth;
-* cpu_baseline -- the FP64 CPU restatement on all host cores, on a bounded
-             sample of the same fields, scaled by relaxations;
+* cpu_baseline -- the reference's own CPU PTP (FP64, every host core) on one
+             field of every mesh up to 400k vertices, scaled by the GPU-counted
+             relaxations of each mesh's fields; the same fields also check the
+             GPU result against the FP64 oracle (oracle_check);
 * clocks, gpu_launches -- SM clocks sampled during the timed region, and the
              library's kernel launches inside it.
 
 Usage: python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+``--impl reference`` times the reference's own CPU PTP (geodesics PTP_CPU:
+toplesets + parallel_toplesets_propagation_coalescence_cpu) on every host
+core over the whole workload: the K timed steps take the fields in a seeded
+order, 256 / K each, so together they solve every field exactly once.
 Under torchrun each rank solves its own 256-field workload (seed offset by
 rank; weak scaling), and rank 0 prints one JSON line.
 
@@ -261,12 +267,14 @@ def run_gpu(args, rank, world, local):
     dist32 = dist_dev.cpu().numpy()
     err = 0.0
     sched_equal = None
+    field_relax = None
     if not args.skip_check:
         fm = [dmesh[mi] for mi, _ in fields]
         fsrc = [[s] for _, s in fields]
         d64s, st64, _ = _capi.ptp_batch(ctx, fm, fsrc, dtype=np.float64, precision=_capi.GP_F64, round_coords=True)
         d32s, st32, _ = _capi.ptp_batch(ctx, fm, fsrc, dtype=np.float32, precision=_capi.GP_F32)
         sched_equal = sum(int(a.n_iter == b.n_iter) for a, b in zip(st32, st64))
+        field_relax = [(int(a.relaxations), int(a.n_iter)) for a in st32]
         for k in range(len(fields)):
             ref = d64s[k]
             a = dist32[voff[k]:voff[k + 1]].astype(np.float64)
@@ -280,12 +288,13 @@ def run_gpu(args, rank, world, local):
             if fin.any():
                 err = max(err, float(np.max(np.abs(a[fin] - ref[fin]) / ref[fin])))
 
-    # plain single-field GPU PTP over the same fields (fewer steps: it is slow)
-    plain_steps = max(1, min(args.steps, 2))
+    # plain single-field GPU PTP over the same fields (5 timed passes after 2
+    # warm-ups: each pass is ~0.8 s)
+    plain_steps = max(1, min(args.steps, 5))
     if args.only_batched:
         ms_plain, pstats = float("nan"), [[]]
     else:
-        ms_plain, pstats = timed(plain, plain_steps, 1, "plain")
+        ms_plain, pstats = timed(plain, plain_steps, 2, "plain")
 
     # e2e with host buffers through the same C entry point
     src_pinned = torch.from_numpy(src_host.view(np.int32)).pin_memory()
@@ -306,6 +315,8 @@ def run_gpu(args, rank, world, local):
         ms_e2e, estats = timed(e2e, args.steps, args.warmup, "e2e")
     same = all(np.array_equal(host_out[k], dist32[voff[k]:voff[k + 1]]) for k in range(F))
 
+    strong = strong_scaling(args, ctx, rank, world, timed) if world > 1 else None
+
     s0 = stats[-1]
     relax_total = int(s0.relax_local + s0.relax_grid)
     return {
@@ -313,45 +324,231 @@ def run_gpu(args, rank, world, local):
         "sched_equal": sched_equal,
         "e2e_stats": estats[-1].as_dict(), "err": err, "e2e_equal": same, "clocks": clocks, "F": F,
         "relax_total": relax_total, "nv_total": int(voff[-1]), "meshes": meshes, "fields": fields,
-        "plain_launches": sum(p.launches for p in pstats[-1]),
+        "field_relax": field_relax, "gpu_dists": [dist32[voff[k]:voff[k + 1]] for k in range(F)],
+        "plain_launches": sum(p.launches for p in pstats[-1]), "plain_steps": plain_steps,
         "grid_kernel": {0: "none", 1: "lockstep", 2: "queue"}.get(int(s0.grid_kernel), "?"),
         "tuned": tuned, "graph": plan is not None, "launches_per_step": int(s0.launches),
+        "strong": strong,
     }
 
 
+def strong_scaling(args, ctx, rank, world, timed):
+    """Strong scaling: the fixed workload of rank 0's seed split across the
+    ranks by the sweep-cost model (gproshan_gb300.shard: strided cost
+    predictions, one all-gather of the costs, longest-predicted-first split),
+    each rank solving its share in one batched call per step with inputs
+    resident; time = max over ranks."""
+    import ctypes as C
+    import torch
+    import torch.distributed as dist
+    from gproshan_gb300 import _capi, shard
+    meshes, fields = make_workload(shard_seed(args.seed, 0), args.meshes)
+    F = len(fields)
+    share = list(range(rank, F, world))
+    dm = {}
+
+    def mesh(mi):
+        if mi not in dm:
+            dm[mi] = _capi.DeviceMesh(ctx, meshes[mi][1], meshes[mi][2])
+        return dm[mi]
+
+    pc = shard.predicted_costs(ctx, [mesh(fields[k][0]) for k in share], [[fields[k][1]] for k in share])
+    got = [None] * world
+    dist.all_gather_object(got, (share, [float(x) for x in pc]))
+    costs = np.zeros(F)
+    for idx, cs in got:
+        costs[idx] = cs
+    parts = shard.lpt_partition(costs, world)
+    mine = parts[rank]
+    dm = {mi: dm[mi] for mi in {fields[k][0] for k in mine} if mi in dm}
+    n = len(mine)
+    src = torch.tensor([fields[k][1] for k in mine] or [0], dtype=torch.int32, device="cuda")
+    nvs = [mesh(fields[k][0]).n_vertices for k in mine]
+    off = np.concatenate([[0], np.cumsum(nvs)]).astype(np.int64)
+    out = torch.empty(max(int(off[-1]), 1), dtype=torch.float32, device="cuda")
+    arr = (_capi.gp_field * max(n, 1))()
+    for q, k in enumerate(mine):
+        arr[q].mesh = mesh(fields[k][0]).handle
+        arr[q].sources = src.data_ptr() + 4 * q
+        arr[q].dist = out.data_ptr() + 4 * int(off[q])
+        arr[q].n_sources = 1
+    opts = _capi.make_opts(_capi.GP_F32, schedule=_capi.GP_SCHED_LEARNED)
+    sec = C.c_double()
+
+    def step():
+        if n:
+            ctx.check(_capi.lib().gp_ptp_batch(ctx.handle, arr, n, C.byref(opts), _capi.GP_F32,
+                                               _capi.GP_BATCH_DEVICE_POINTERS, C.byref(sec)), "gp_ptp_batch")
+        return None
+
+    ms, _ = timed(step, args.steps, args.warmup, "strong")
+    return {"value": F / (ms * 1e-3), "unit": "fields/s", "ms_per_step": ms, "fields": F,
+            "fields_per_rank": [len(p) for p in parts],
+            "predicted_relaxations_per_rank": [float(sum(costs[k] for k in p)) for p in parts],
+            "what": "the fixed workload (rank 0's seed) split across the ranks by predicted cost, "
+                    "longest-predicted-first; max time over ranks"}
+
+
 # --------------------------------------------------------------------------
-# CPU: the oracle port (or the reference build) on a bounded sample
+# CPU: the reference's own CPU PTP (or, without its sources, the oracle port)
 # --------------------------------------------------------------------------
-def cpu_sample(meshes, fields, budget_s: float, max_nv: int = 300_000, start: int = 0):
-    """Time the CPU PTP (the FP64 oracle port, OpenMP on every host core) on
-    fields in workload order, skipping meshes above max_nv so that one field
-    stays within the budget, until budget_s elapses.
-    Returns (relaxations, seconds, n_fields, kind, threads)."""
+class CpuPtp:
+    """One field on the host cores the way geodesics(mesh, sources, PTP_CPU)
+    computes it: toplesets, then parallel_toplesets_propagation_coalescence_cpu
+    (reference src/geodesics.cpp:192-207, src/geodesics_ptp.cpp:40-120), FP64,
+    OpenMP on every host core.  kind "reference": the reference's own code
+    compiled by oracle/Makefile (oracle/_ref); kind "port": the oracle's C
+    restatement when the reference's sources are not at hand.  Meshes are
+    built once, outside any timed region, on the float-rounded coordinates the
+    FP32 GPU path reads."""
+
+    def __init__(self, meshes):
+        import oracle
+        oracle.build()
+        self.threads = os.cpu_count() or 1
+        self.meshes = meshes
+        self.cache = {}
+        try:
+            self.L = oracle.RefLib("f64")
+            self.kind = "reference"
+        except (FileNotFoundError, OSError):
+            self.L = None
+            self.kind = "port"
+
+    def mesh(self, mi):
+        import oracle
+        if mi not in self.cache:
+            _, xyz, tri = self.meshes[mi]
+            x = np.asarray(xyz, dtype=np.float32).astype(np.float64)
+            self.cache[mi] = oracle.RefMesh(self.L, x, tri) if self.L else oracle.Mesh(x, tri)
+        return self.cache[mi]
+
+    def solve(self, mi, src):
+        import oracle
+        m = self.mesh(mi)
+        if self.L:
+            return m.geodesics_ptp_cpu([src])
+        _, srt, lim = oracle.toplesets(m, [src])
+        return oracle.ptp(m, [src], lim, srt, nthreads=self.threads)["dist_cpu"]
+
+
+def reference_order(n_fields: int, seed: int):
+    """The order in which the reference arm's steps take the workload's
+    fields: a seeded permutation, so every step mixes mesh sizes."""
+    return np.random.default_rng(seed + 99).permutation(n_fields)
+
+
+def cpu_baseline_sample(meshes, fields, field_relax, gpu_dists, max_nv: int = 400_000):
+    """The GPU arm's CPU baseline and oracle check, on a bounded sample:
+    one field of every mesh with at most max_nv vertices (every family and
+    size class of the workload up to the 587^2 height field).
+
+    * baseline: each sampled field is timed on the reference's CPU PTP; the
+      mesh's measured rate (relaxations/s, relaxations counted on the GPU,
+      which runs the same schedule) times the GPU-counted relaxations of all
+      of that mesh's fields gives the mesh's CPU time; the few larger meshes
+      take the rate of the largest sampled mesh of their family.
+    * oracle check: the same fields on the oracle port (FP64, float-rounded
+      coordinates): the GPU FP32 result against the GPU-returned buffer
+      (max rel. error, sweep counts), and the port's CPU-returned buffer
+      against the reference's output bit for bit."""
     import oracle
-    threads = os.cpu_count() or 1
-    relax = 0
-    t_total = 0.0
-    n = 0
-    cache = {}
-    k = start
-    tried = 0
-    while t_total < budget_s and tried < len(fields):
-        mi, s = fields[k % len(fields)]
-        k += 1
-        tried += 1
-        name, xyz, tri = meshes[mi]
-        if len(xyz) > max_nv:
-            continue
-        if mi not in cache:
-            cache[mi] = oracle.Mesh(xyz, tri)
-        m = cache[mi]
-        _, srt, lim = oracle.toplesets(m, [s])
+    cpu = CpuPtp(meshes)
+    first = {}
+    for k, (mi, s) in enumerate(fields):
+        first.setdefault(mi, k)
+    sampled = [k for mi, k in sorted(first.items()) if len(meshes[mi][1]) <= max_nv]
+    rate = {}
+    t_sample = 0.0
+    r_sample = 0
+    err = 0.0
+    same_ref = 0
+    sweeps_equal = 0
+    for k in sampled:
+        mi, s = fields[k]
+        cpu.mesh(mi)
         t = time.perf_counter()
-        out = oracle.ptp(m, [s], lim, srt, nthreads=threads)
-        t_total += time.perf_counter() - t
-        relax += out["relaxations"]
-        n += 1
-    return relax, t_total, n, "port", threads
+        d_cpu = cpu.solve(mi, s)
+        dt = time.perf_counter() - t
+        t_sample += dt
+        r_sample += field_relax[k][0]
+        rate[mi] = field_relax[k][0] / dt if dt > 0 else float("inf")
+        om = oracle.Mesh(np.asarray(meshes[mi][1], np.float32).astype(np.float64), meshes[mi][2])
+        _, srt, lim = oracle.toplesets(om, [s])
+        o = oracle.ptp(om, [s], lim, srt, nthreads=cpu.threads)
+        err = max(err, oracle.max_rel_err(gpu_dists[k], o["dist"]))
+        sweeps_equal += int(o["n_iter"] == field_relax[k][1])
+        same_ref += int(np.array_equal(o["dist_cpu"], d_cpu))
+        cpu.cache.pop(mi, None)
+    fam_rate = {}
+    for mi in rate:  # the largest sampled mesh of each family
+        fam = meshes[mi][0][:3]
+        if fam not in fam_rate or len(meshes[mi][1]) > len(meshes[fam_rate[fam]][1]):
+            fam_rate[fam] = mi
+    t_total = 0.0
+    scaled = set()
+    for k, (mi, _) in enumerate(fields):
+        r = rate.get(mi)
+        if r is None:
+            r = rate[fam_rate[meshes[mi][0][:3]]]
+            scaled.add(mi)
+        t_total += field_relax[k][0] / r
+    v = len(fields) / t_total if t_total else 0.0
+    big = ", ".join(f"{meshes[mi][0].split('_')[0]}" for mi in sorted(scaled))
+    base = {"value": v, "unit": "fields/s", "cores": cpu.threads, "kind": cpu.kind,
+            "sample": f"{len(sampled)} fields, one per mesh of <= {max_nv} vertices ({r_sample} relaxations, "
+                      f"{t_sample:.1f} s timed); each mesh's measured rate x the GPU-counted relaxations of its "
+                      f"fields; {len(scaled)} larger meshes ({big}) at the rate of the largest sampled mesh of "
+                      f"their family",
+            "estimate": True}
+    check = {"fields": len(sampled), "max_rel_err_vs_oracle": err, "sweeps_equal_oracle": sweeps_equal,
+             "oracle_cpu_buffer_equals_reference": same_ref if cpu.kind == "reference" else None,
+             "what": "GPU FP32 result vs the FP64 oracle on the same float-rounded coordinates; the oracle's "
+                     "CPU-returned buffer vs the reference's own CPU PTP output (bit for bit)"}
+    return base, check
+
+
+def reference_arm(args):
+    """`--impl reference`: the reference's CPU PTP on the host cores over the
+    whole workload.  The timed steps take the workload's fields in a seeded
+    order, step k the fields [k F / K, (k + 1) F / K) of it, so the K timed
+    steps together solve every field exactly once; value = fields / total
+    time.  Warm-up steps solve one small field each."""
+    meshes, fields = make_workload(shard_seed(args.seed, 0), args.meshes)
+    cpu = CpuPtp(meshes)
+    for mi in range(len(meshes)):
+        cpu.mesh(mi)
+    F = len(fields)
+    order = reference_order(F, args.seed)
+    small = min(range(F), key=lambda k: len(meshes[fields[k][0]][1]))
+    for _ in range(args.warmup):
+        cpu.solve(*fields[small])
+    K = max(args.steps, 1)
+    times = []
+    n = 0
+    for step in range(K):
+        ks = [int(order[q]) for q in range(step * F // K, (step + 1) * F // K)]
+        t = time.perf_counter()
+        for k in ks:
+            cpu.solve(*fields[k])
+        times.append(time.perf_counter() - t)
+        n += len(ks)
+    T = sum(times)
+    v = n / T if T else 0.0
+    desc = ("the reference's own parallel_toplesets_propagation_coalescence_cpu + che::compute_toplesets "
+            "(oracle/_ref, built from its unmodified sources)" if cpu.kind == "reference" else
+            "the oracle's C restatement of the reference CPU PTP (reference sources not present)")
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": "fields/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * T / max(args.steps, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic",
+            "config": {"workload": WORKLOAD, "fields": F, "vertices_per_step": int(sum(len(meshes[mi][1])
+                                                                                        for mi, _ in fields)),
+                       "parallelism": f"cpu x{cpu.threads} threads"},
+            "cpu_baseline": {"value": v, "unit": "fields/s", "cores": cpu.threads, "kind": cpu.kind,
+                             "sample": f"all {F} fields of the workload, about {F // K} per timed step ({n} solved in "
+                                       f"{T:.1f} s): {desc}, FP64, OpenMP on every host core"},
+            "e2e": {"value": v, "unit": "fields/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
 def emit(obj):
@@ -365,7 +562,6 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--seed", type=int, default=2024)
-    ap.add_argument("--cpu-budget", type=float, default=15.0)
     ap.add_argument("--skip-check", action="store_true")
     ap.add_argument("--meshes", type=int, default=N_MESHES, help="meshes in the workload (profiling runs)")
     ap.add_argument("--only-batched", action="store_true", help="skip the plain, e2e and CPU legs (profiling runs)")
@@ -391,33 +587,8 @@ def main():
         dist.init_process_group(backend)
 
     if args.impl == "reference":
-        if rank != 0:
-            return
-        meshes, fields = make_workload(shard_seed(args.seed, 0), args.meshes)
-        # total relaxations of the workload, from the oracle's schedule on the
-        # fields the sample covers, scaled by vertex count for the rest
-        per_step = []
-        kinds = None
-        start = 0
-        for step in range(args.warmup + args.steps):
-            r, t, n, kind, thr = cpu_sample(meshes, fields, args.cpu_budget / 3, start=start)
-            start += n
-            kinds = (kind, thr, n)
-            if step >= args.warmup:
-                per_step.append((r, t))
-        R = sum(r for r, _ in per_step)
-        T = sum(t for _, t in per_step)
-        rate = R / T if T else 0.0
-        est_total = estimate_total_relax(meshes, fields)
-        v = len(fields) * rate / est_total if est_total else 0.0
-        emit({"impl": "reference", "metric": METRIC, "value": v, "unit": "fields/s", "n_gpus": args.gpus,
-              "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * len(fields) / v if v else None,
-              "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-              "data": "synthetic", "config": {"workload": WORKLOAD, "fields": len(fields), "parallelism": "cpu"},
-              "cpu_baseline": {"value": v, "unit": "fields/s", "cores": kinds[1], "kind": kinds[0],
-                               "sample": f"{R} vertex relaxations over {T:.1f} s on fields of meshes <=300k "
-                                         f"vertices, scaled to the workload's estimated {est_total:.3g}"},
-              "e2e": {"value": v, "unit": "fields/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}})
+        if rank == 0:
+            emit(reference_arm(args))
         return
 
     res = run_gpu(args, rank, world, local)
@@ -445,15 +616,10 @@ def main():
         t = json.load(open(tp)).get(kname.split()[0])
         if t and t.get("dram_bytes_per_relax"):
             traffic = t["dram_bytes_per_relax"] * krelax
-    # CPU baseline on a bounded sample (rank 0, N=1 only)
-    cpu = None
-    if world == 1 and not args.only_batched:
-        r, t, n, kind, thr = cpu_sample(res["meshes"], res["fields"], args.cpu_budget)
-        rate = r / t if t else 0.0
-        cpu_v = res["F"] * rate / res["relax_total"] if res["relax_total"] else 0.0
-        cpu = {"value": cpu_v, "unit": "fields/s", "cores": thr, "kind": kind,
-               "sample": f"{n} fields of meshes <=300k vertices ({r} relaxations, {t:.1f} s, FP64 oracle port "
-                         f"with OpenMP); rate scaled to the workload's {res['relax_total']} relaxations"}
+    # CPU baseline and oracle check on a bounded sample (rank 0, N=1 only)
+    cpu, ocheck = None, None
+    if world == 1 and not args.only_batched and res["field_relax"] is not None:
+        cpu, ocheck = cpu_baseline_sample(res["meshes"], res["fields"], res["field_relax"], res["gpu_dists"])
     launches = res["launches_per_step"] * args.steps
     out = {
         "metric": METRIC, "value": value, "unit": "fields/s", "n_gpus": world, "steps": args.steps,
@@ -467,12 +633,13 @@ def main():
                    "schedule": args.schedule, "grid_kernel": res["grid_kernel"], "autotuned": res["tuned"],
                    "cuda_graph": res["graph"],
                    "l2": "inputs larger than L2 (129 MB): the step touches every mesh and field buffer"},
-        "plain": {"value": plain, "unit": "fields/s", "ms_per_step": res["ms_plain"],
+        "plain": {"value": plain, "unit": "fields/s", "ms_per_step": res["ms_plain"], "steps": res["plain_steps"],
                   "what": "same fields, one gp_ptp_batch call per field (single-field GPU PTP)"},
         "batched_over_plain": value / plain,
         "max_rel_err": res["err"],
         "max_rel_err_vs": "FP64 reference-formula run of the same fields on the same float-rounded coordinates",
         "fields_same_sweep_count": res["sched_equal"],
+        "oracle_check": ocheck,
         "e2e": {"value": e2e, "unit": "fields/s", "h2d_bytes_per_step": res["e2e_stats"]["h2d_bytes"],
                 "d2h_bytes_per_step": res["e2e_stats"]["d2h_bytes"], "ms_per_step": res["ms_e2e"],
                 "equal_to_device_run": res["e2e_equal"]},
@@ -483,6 +650,7 @@ def main():
         "phases_ms": {k: statistics.mean(s[k] for s in st) for k in
                       ("ms_toplesets", "ms_renumber", "ms_local", "ms_grid", "ms_gather")},
         "cpu_baseline": cpu,
+        "strong_scaling": res["strong"],
         "clocks": res["clocks"],
         "gpu_launches": launches,
     }
@@ -569,18 +737,6 @@ def run_config(args):
                     "config": {"workload": "bump field 1414^2 (1,999,396 vertices), 64 Gaussian bumps, 5% "
                                            "displaced vertices; farthest-point sampling from vertex 0"}})
     return rec
-
-
-def estimate_total_relax(meshes, fields):
-    """Relaxations of the whole workload from a schedule model fitted to the
-    oracle on small meshes: about 3 V per icosphere field and 0.27 V^1.5 per
-    height-field field (fits the reference schedule within tens of percent)."""
-    tot = 0.0
-    for mi, _ in fields:
-        name, xyz, _ = meshes[mi]
-        n = len(xyz)
-        tot += 3.0 * n if name.startswith("ico") else 0.27 * n ** 1.5
-    return tot
 
 
 if __name__ == "__main__":

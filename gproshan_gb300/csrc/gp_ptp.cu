@@ -235,8 +235,13 @@ __device__ __forceinline__ void take32(const Nb32 &a, const Nb32 &b, Cand32 &bes
 	if(c.p < best.p)
 	{
 		best = c;
-		// GPU label rule (src/cuda/geodesics_ptp.cu:277): a = x0 (next), b = x1 (prev)
-		if(CL) lab = b.t < a.t ? ld_d<uint32_t, COH>(Co + b.u) : ld_d<uint32_t, COH>(Co + a.u);
+		// GPU label rule (src/cuda/geodesics_ptp.cu:277): a = x0 (next), b = x1
+		// (prev); the old distances compared exactly, as (t, te) pairs
+		if(CL)
+		{
+			const bool pb = b.t < a.t || (b.t == a.t && b.te < a.te);
+			lab = pb ? ld_d<uint32_t, COH>(Co + b.u) : ld_d<uint32_t, COH>(Co + a.u);
+		}
 	}
 }
 
@@ -1463,23 +1468,9 @@ __global__ void fill_kernel(CatArgs c)
 						F.fan[dst + q] = x;
 					}
 				if(n > 8) r[7] = FAN8_OVERFLOW;
-				// FP32 path only (the FP64 path keeps the reference's triangle order,
-				// so its labels follow the reference's tie rule bit for bit):
-				// start a closed star one before its lowest-numbered neighbour, the
-				// one nearest the sources in ring order, so the two triangles around
-				// it, usually the upwind ones, come first.  The distances do not
-				// depend on the order except through exact ties of rounded
-				// candidates; a fixed rule keeps the labels of those ties the same
-				// with and without the label field.
-				if(sizeof(T) == 4 && n >= 3 && n <= 8 && (o0f & FAN_CLOSED))
-				{
-					uint32_t m = 0;
-					for(uint32_t q = 1; q < n; q++)
-						if(r[q] < r[m]) m = q;
-					uint32_t t[8];
-					for(uint32_t q = 0; q < 8; q++) t[q] = q < n ? r[(q + m + n - 1) % n] : r[q];
-					for(uint32_t q = 0; q < 8; q++) r[q] = t[q];
-				}
+				// the star keeps the reference's triangle order (che::link from
+				// EVT), so the label rule's "first strictly smaller candidate"
+				// picks the same triangle as the reference in exact ties
 				if(n && (o0f & FAN_CLOSED)) r[0] |= FAN_CLOSED;
 				F.fan8[2 * (size_t) k] = make_uint4(r[0], r[1], r[2], r[3]);
 				F.fan8[2 * (size_t) k + 1] = make_uint4(r[4], r[5], r[6], r[7]);

@@ -28,14 +28,34 @@ _f64p = np.ctypeslib.ndpointer(dtype=np.float64, flags="C_CONTIGUOUS")
 _f32p = np.ctypeslib.ndpointer(dtype=np.float32, flags="C_CONTIGUOUS")
 
 
-def build(ref: bool = False, ref_dir: str | None = None) -> None:
-    """Compile the oracle (and, with ``ref``, the reference's own CPU code)."""
+STAGED_REF = os.path.join(HERE, "..", "baseline", "_ref")
+
+
+def reference_sources() -> str | None:
+    """Where the reference's CPU sources are: a checkout named by the
+    GPROSHAN_REF environment variable, else the staged copy under
+    baseline/_ref/ (see the Makefile's ``stage`` target), else None."""
+    env = os.environ.get("GPROSHAN_REF")
+    for d in (env, STAGED_REF):
+        if d and os.path.isfile(os.path.join(d, "src", "geodesics_ptp.cpp")):
+            return os.path.abspath(d)
+    return None
+
+
+def build(ref: bool | None = None, ref_dir: str | None = None) -> None:
+    """Compile the oracle and, when the reference's sources are at hand
+    (``ref_dir``, GPROSHAN_REF or the staged copy), the reference's own CPU
+    code into _ref/.  With GPROSHAN_REF set, its sources are first staged
+    into baseline/_ref/ so that they travel with the working tree."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
-    if ref:
-        args = ["make", "-s", "-C", HERE, "ref"]
-        if ref_dir:
-            args.append(f"REF={ref_dir}")
-        subprocess.run(args, check=True)
+    env = os.environ.get("GPROSHAN_REF")
+    if env and os.path.isfile(os.path.join(env, "src", "geodesics_ptp.cpp")):
+        subprocess.run(["make", "-s", "-C", HERE, "stage", f"GPROSHAN_REF={env}"], check=True)
+    src = ref_dir or reference_sources()
+    if ref is None:
+        ref = src is not None
+    if ref and src:
+        subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
 
 
 class _OrcInfo(C.Structure):
@@ -231,6 +251,9 @@ class RefLib:
         self.upd = getattr(L, p + "update_step")
         self.upd.restype = C.c_double if precision == "f64" else C.c_float
         self.upd.argtypes = [C.c_void_p, rp, C.c_uint]
+        self.geod = getattr(L, p + "geodesics_ptp_cpu")
+        self.geod.restype = C.c_uint
+        self.geod.argtypes = [C.c_void_p, _u32p, C.c_uint, rp]
         self.norm = getattr(L, p + "normalize_ptp")
         self.norm.argtypes = [rp, C.c_ulonglong]
         self.off_open = getattr(L, p + "off_open")
@@ -301,6 +324,14 @@ class RefMesh:
         self.L.ptp_cpu(self.h, src, len(src), _u32(limits), len(limits), _u32(sorted_), dist,
                        cl.ctypes.data if cl is not None else None, int(coalescence))
         return (dist, cl) if clusters is not None else dist
+
+    def geodesics_ptp_cpu(self, sources, out=None):
+        """One field as geodesics(mesh, sources, PTP_CPU) computes it:
+        toplesets + the coalescence CPU PTP (the reference's CPU timing unit)."""
+        src = _u32(sources)
+        dist = np.empty(self.nv, self.L.real) if out is None else out
+        self.L.geod(self.h, src, len(src), dist)
+        return dist
 
     def update_step(self, dist, he):
         return self.L.upd(self.h, np.ascontiguousarray(dist, dtype=self.L.real), he)

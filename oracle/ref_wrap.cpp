@@ -14,6 +14,8 @@
  *                                           src/geodesics_ptp.cpp:40-120
  *   - update_step                           src/geodesics_ptp.cpp:201-262
  *   - normalize_ptp                         src/geodesics_ptp.cpp:264-276
+ *   - geodesics(mesh, sources, PTP_CPU)     src/geodesics.cpp:16-33, 192-207
+ *     (one field end to end: toplesets, then the coalescence CPU PTP)
  *   - che_off(file) (OFF reader)            src/che_off.cpp:28-79
  *
  * Built twice: once with real_t = double (the reference default) and once
@@ -24,6 +26,7 @@
 #include "che_off.h"
 #include "geodesics_ptp.h"
 
+#include <cmath>
 #include <cstring>
 #include <vector>
 
@@ -140,6 +143,28 @@ void REFW(ptp_cpu)(void * h, const unsigned * src, unsigned n_src,
 		gproshan::parallel_toplesets_propagation_coalescence_cpu(out, m, sources, ts);
 	else
 		gproshan::parallel_toplesets_propagation_cpu(out, m, sources, ts);
+}
+
+/*
+ * One field the way geodesics(mesh, sources, PTP_CPU) computes it
+ * (src/geodesics.cpp:16-33 and run_parallel_toplesets_propagation_cpu,
+ * :192-207): dist set to INFINITY, che::compute_toplesets, then
+ * parallel_toplesets_propagation_coalescence_cpu.  The timed unit of the
+ * CPU baselines.  Returns the number of limits.
+ */
+unsigned REFW(geodesics_ptp_cpu)(void * h, const unsigned * src, unsigned n_src, distance_t * dist)
+{
+	che * m = (che *) h;
+	const size_t n = m->n_vertices();
+	for(size_t v = 0; v < n; v++)
+		dist[v] = INFINITY;
+	std::vector<index_t> sources(src, src + n_src);
+	std::vector<index_t> toplesets(n), sorted(n + n_src), limits;
+	index_t * r = toplesets.data();
+	index_t * s = sorted.data();
+	m->compute_toplesets(r, s, limits, sources);
+	gproshan::parallel_toplesets_propagation_coalescence_cpu({dist, nullptr}, m, sources, {limits, s});
+	return (unsigned) limits.size();
 }
 
 distance_t REFW(update_step)(void * h, const distance_t * dist, unsigned he)

@@ -161,6 +161,68 @@ def test_duplicate_and_isolated_sources(gpu_ctx, oracle_lib):
     assert st.n_iter == ref["n_iter"] and np.array_equal(d, ref["dist"])
 
 
+def test_icosphere_l6_workload_exact(gpu_ctx, oracle_lib):
+    """The single-field workload exactly as specified: icosphere subdivided 6
+    times (40,962 vertices, 81,920 faces, unit radius), vertices jittered
+    tangentially by seeded uniform noise of 0.1 x mean edge, source vertex 0.
+    FP64: the same sweeps, relaxations and distance bits as the oracle; FP32:
+    within 1e-5 of the FP64 oracle on the same float-rounded coordinates, with
+    the same sweep count.  Where the reference's own CPU build is present, the
+    oracle's CPU-returned buffer equals its output bit for bit as well."""
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.icosphere(6, 0.1, 0)
+    assert len(xyz) == 40962 and len(tri) == 81920
+    assert np.allclose(np.linalg.norm(xyz, axis=1), 1.0)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    r_o, s_o, l_o = oracle_lib.toplesets(om, [0])
+    rings, srt, lim = _capi.toplesets(m, [0])
+    assert np.array_equal(rings, r_o) and np.array_equal(srt, s_o) and np.array_equal(lim, l_o)
+    ref64 = oracle_lib.ptp(om, [0], l_o, s_o)
+    d64, _, st64 = _capi.ptp(m, [0], dtype=np.float64, precision=_capi.GP_F64)
+    assert st64.n_iter == ref64["n_iter"] == 194 and st64.relaxations == ref64["relaxations"]
+    assert np.array_equal(d64, ref64["dist"])
+    x32 = xyz.astype(np.float32).astype(np.float64)
+    ref32 = oracle_lib.ptp(om, [0], l_o, s_o, xyz=x32)
+    d32, _, st32 = _capi.ptp(m, [0])
+    assert st32.n_iter == ref32["n_iter"]
+    assert oracle_lib.max_rel_err(d32, ref32["dist"]) <= REL_TOL_F32
+    try:
+        rl = oracle_lib.RefLib("f64")
+    except (FileNotFoundError, OSError):
+        return
+    rm = oracle_lib.RefMesh(rl, xyz, tri)
+    assert np.array_equal(rm.geodesics_ptp_cpu([0]), ref64["dist_cpu"])
+
+
+@pytest.mark.parametrize("maker,src", [
+    (lambda mg: mg.icosphere(4, 0.1, 2), [0, 1000, 2000]),
+    (lambda mg: mg.icosphere(5, 0.1, 7), [3, 500, 4000, 9000, 10000]),
+    (lambda mg: mg.height_field(90, 4), [0, 4000, 8099]),
+    (lambda mg: mg.torus(80, 200, seed=1), [10, 5000, 11000, 15999]),
+])
+def test_fp32_labels_follow_the_reference_rule(gpu_ctx, oracle_lib, maker, src):
+    """FP32 labels are integer output: the label of the first strictly smaller
+    candidate in the reference's star order, taken from the nearer of the
+    triangle's two other vertices (src/cuda/geodesics_ptp.cu:257-282).  They
+    equal the FP64 oracle's labels bit for bit (same float-rounded
+    coordinates), every source labelled with its 1-based index, on every launch
+    kind; and labelling leaves the FP32 distances unchanged."""
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = maker(meshgen)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    ref = oracle_lib.ptp(om, src, clusters=True, xyz=xyz.astype(np.float32).astype(np.float64))
+    plain, _, _ = _capi.ptp(m, src)
+    for kw in (dict(local_window=1 << 30), dict(local_window=1, grid_kernel=_capi.GP_GRID_LOCKSTEP),
+               dict(local_window=1, grid_kernel=_capi.GP_GRID_QUEUE, queue_min=1)):
+        d, cl, st = _capi.ptp(m, src, clusters=np.zeros(len(xyz), np.uint32), opts=_capi.make_opts(0, **kw))
+        assert st.n_iter == ref["n_iter"]
+        assert np.array_equal(cl, ref["clusters"]), (kw, int(np.sum(cl != ref["clusters"])))
+        assert np.array_equal(d, plain)
+    assert [int(cl[s]) for s in src] == list(range(1, len(src) + 1))
+
+
 def test_clusters_gpu_rule(gpu_ctx, oracle_lib):
     from gproshan_gb300 import _capi, meshgen
     xyz, tri = meshgen.icosphere(4, 0.1, 2)

@@ -101,9 +101,11 @@ def test_cpp_dropin_shim_compiles_against_reference_headers():
     the reference's own headers (FP64 and SINGLE_P builds)."""
     import shutil
     import subprocess
-    ref = "/root/reference/include"
-    if not os.path.isdir(ref) or not shutil.which("g++"):
-        pytest.skip("reference checkout or g++ not present")
+    import oracle
+    src = oracle.reference_sources()
+    if src is None or not shutil.which("g++"):
+        pytest.skip("reference sources (GPROSHAN_REF or the staged copy) or g++ not present")
+    ref = os.path.join(src, "include")
     shim = os.path.join(ROOT, "gproshan_gb300", "shim", "geodesics_ptp_gb300.cpp")
     for extra in ([], ["-DSINGLE_P"]):
         r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-fopenmp", *extra,
