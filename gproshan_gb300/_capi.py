@@ -79,6 +79,7 @@ SIGNATURES = {
     "gp_status_str": (C.c_char_p, [C.c_int]),
     "gp_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "gp_ctx_workspace_bytes": (C.c_size_t, [C.c_void_p]),
+    "gp_ctx_device_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gp_che_build": (C.c_int, [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.POINTER(C.c_int)]),
     "gp_mesh_create": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_void_p, C.c_void_p,
@@ -218,6 +219,12 @@ class Context:
         cs = gp_call_stats()
         self.check(lib().gp_ctx_call_stats(self._h, C.byref(cs)), "gp_ctx_call_stats")
         return cs
+
+    def device_info(self):
+        """(compute capability, binary version of the loaded sweep kernel, SMs)."""
+        cc, bv, ns = C.c_int(), C.c_int(), C.c_int()
+        self.check(lib().gp_ctx_device_info(self._h, C.byref(cc), C.byref(bv), C.byref(ns)), "gp_ctx_device_info")
+        return cc.value, bv.value, ns.value
 
     def arm_step_trace(self, cap: int):
         self.check(lib().gp_ctx_step_trace(self._h, cap, None, None), "gp_ctx_step_trace")

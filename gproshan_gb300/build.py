@@ -7,7 +7,9 @@ from this directory by ``gproshan_gb300._capi``.
 from __future__ import annotations
 
 import concurrent.futures as cf
+import hashlib
 import os
+import platform
 import shutil
 import subprocess
 import sys
@@ -16,6 +18,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libgp_ptp.so")
+STAMP = LIB + ".stamp"  # fingerprint of what LIB was built from (see _fingerprint)
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O3",
@@ -44,19 +47,39 @@ def _compile(src: str, verbose_ptxas: bool) -> str:
     return obj
 
 
-def _stale() -> bool:
-    if not os.path.exists(LIB):
+def _fingerprint() -> str:
+    """sha256 of everything the library is built from: every source under
+    csrc/, the public header, this script (flags and source list), the nvcc
+    version and the machine type."""
+    h = hashlib.sha256()
+    files = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC))
+    files += [os.path.join(HERE, "..", "include", "gp_ptp.h"), os.path.abspath(__file__)]
+    for p in files:
+        if os.path.isfile(p):
+            h.update(os.path.basename(p).encode())
+            with open(p, "rb") as f:
+                h.update(f.read())
+    r = subprocess.run([nvcc(), "--version"], capture_output=True, text=True)
+    h.update(r.stdout.encode())
+    h.update(platform.machine().encode())
+    return h.hexdigest()
+
+
+def _stale(fp: str) -> bool:
+    """The library is rebuilt unless it exists beside a stamp holding the
+    fingerprint of the sources, flags, toolchain and machine it came from (a
+    copy built elsewhere, or from other sources, is never reused)."""
+    if not os.path.exists(LIB) or not os.path.exists(STAMP):
         return True
-    t = os.path.getmtime(LIB)
-    deps = [os.path.join(CSRC, f) for f in os.listdir(CSRC)]
-    deps.append(os.path.join(HERE, "..", "include", "gp_ptp.h"))
-    deps.append(os.path.abspath(__file__))
-    return any(os.path.getmtime(d) > t for d in deps if os.path.exists(d))
+    with open(STAMP) as f:
+        return f.read().strip() != fp
 
 
 def build(force: bool = False, verbose_ptxas: bool = False) -> str:
-    """Compile libgp_ptp.so if any source is newer than it; return its path."""
-    if not force and not _stale():
+    """Compile libgp_ptp.so unless its stamp matches the current fingerprint;
+    return its path."""
+    fp = _fingerprint()
+    if not force and not _stale(fp):
         return LIB
     os.makedirs(BUILD, exist_ok=True)
     with cf.ThreadPoolExecutor(max_workers=len(SOURCES)) as ex:
@@ -67,6 +90,8 @@ def build(force: bool = False, verbose_ptxas: bool = False) -> str:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    with open(STAMP, "w") as f:
+        f.write(fp + "\n")
     return LIB
 
 

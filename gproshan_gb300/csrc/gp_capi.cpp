@@ -44,6 +44,7 @@ cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fie
                              uint32_t min_queue, uint32_t tile, bool f64, bool clusters, cudaStream_t s);
 int ptp_queue_max_ctas(int device, bool f64, bool clusters);
 uint32_t ptp_grid_max_fields();
+int ptp_binary_version();
 } // namespace gp
 
 using namespace gp;
@@ -807,6 +808,19 @@ gp_status gp_ctx_call_stats(const gp_ctx *ctx, gp_call_stats *out)
 }
 void *gp_ctx_stream(gp_ctx *ctx) { return ctx ? (void *) ctx->stream : nullptr; }
 size_t gp_ctx_workspace_bytes(const gp_ctx *ctx) { return ctx ? ctx->ws_bytes : 0; }
+
+gp_status gp_ctx_device_info(const gp_ctx *ctx, int *cc, int *binary_version, int *num_sms)
+{
+	if(!ctx) return GP_ERR_INVALID_ARG;
+	GP_CUDA(const_cast<gp_ctx *>(ctx), cudaSetDevice(ctx->device));
+	int major = 0, minor = 0;
+	cudaDeviceGetAttribute(&major, cudaDevAttrComputeCapabilityMajor, ctx->device);
+	cudaDeviceGetAttribute(&minor, cudaDevAttrComputeCapabilityMinor, ctx->device);
+	if(cc) *cc = 10 * major + minor;
+	if(binary_version) *binary_version = ptp_binary_version();
+	if(num_sms) *num_sms = ctx->num_sms;
+	return GP_OK;
+}
 
 gp_status gp_che_build(uint32_t nv, uint32_t nf, const uint32_t *VT, uint32_t *OT, uint32_t *EVT, int *manifold)
 {

@@ -1702,6 +1702,18 @@ cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fie
 
 uint32_t ptp_grid_max_fields() { return GRID_MAX_FIELDS; }
 
+// binaryVersion of the FP32 sweep kernel's loaded code on the current device
+int ptp_binary_version()
+{
+	cudaFuncAttributes a{};
+	if(cudaFuncGetAttributes(&a, ptp_kernel_ptr(false, false)) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return 0;
+	}
+	return a.binaryVersion;
+}
+
 // notok: 3 * n_fields words; bar: 4 words.  Both zeroed here.
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,

@@ -585,9 +585,12 @@ __global__ void noalloc_finish_kernel(uint32_t *n_limits)
 std::mutex g_noalloc_mu;
 void *g_noalloc_ptr[64] = {};
 
-// Device address of the array on the current device, looked up once per
-// device (the symbol's host-side name is not a device address).
-gp_status noalloc_scratch(void **out)
+// Device address of the array on the current device (the symbol's host-side
+// name is not a device address).  Looked up again on every call made outside
+// stream capture, so that a device reset between calls (which unloads and
+// reloads this module) never leaves a stale address; a call made while `s` is
+// being captured reuses the address of the last uncaptured call on the device.
+gp_status noalloc_scratch(cudaStream_t s, void **out)
 {
 	int dev = -1;
 	if(cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64)
@@ -595,8 +598,14 @@ gp_status noalloc_scratch(void **out)
 		cudaGetLastError();
 		return GP_ERR_NO_DEVICE;
 	}
+	cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+	if(cudaStreamIsCapturing(s, &cs) != cudaSuccess)
+	{
+		cudaGetLastError();
+		cs = cudaStreamCaptureStatusActive;  // cannot tell: treat as capturing
+	}
 	std::lock_guard<std::mutex> lock(g_noalloc_mu);
-	if(!g_noalloc_ptr[dev])
+	if(cs == cudaStreamCaptureStatusNone)
 	{
 		void *p = nullptr;
 		const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -607,6 +616,8 @@ gp_status noalloc_scratch(void **out)
 		}
 		g_noalloc_ptr[dev] = p;
 	}
+	else if(!g_noalloc_ptr[dev])
+		return GP_ERR_INVALID_ARG;  // the first call on a device must come before any capture
 	*out = g_noalloc_ptr[dev];
 	return GP_OK;
 }
@@ -631,11 +642,11 @@ extern "C" gp_status gp_toplesets_noalloc(const gp_mesh *mesh, const uint32_t *s
 		cudaGetLastError();
 		return GP_ERR_INVALID_ARG;  // the mesh's device must be current
 	}
+	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	void *base = nullptr;
-	const gp_status st = noalloc_scratch(&base);
+	const gp_status st = noalloc_scratch(s, &base);
 	if(st != GP_OK) return st;
 	NoallocHeader *h = static_cast<NoallocHeader *>(base);
-	cudaStream_t s = static_cast<cudaStream_t>(stream);
 	noalloc_setup_kernel<<<1, 32, 0, s>>>(*m, sources, n_sources, rings, sorted, cap_sorted, limits);
 	bfs_clear_kernel<<<(unsigned) std::min<uint32_t>((m->nv + 255) / 256, 152 * 16), 256, 0, s>>>(&h->f, h->vbase, 1,
 	                                                                                              m->nv);

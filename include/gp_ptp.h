@@ -61,6 +61,11 @@ const char *gp_status_str(gp_status s);
 void *gp_ctx_stream(gp_ctx *ctx);
 /* Bytes of device workspace currently held by the context. */
 size_t gp_ctx_workspace_bytes(const gp_ctx *ctx);
+/* The context's device and the code loaded for it: compute capability
+ * (10 * major + minor), the binary version of the sweep kernel's loaded code
+ * (cudaFuncGetAttributes; 103 = native sm_103 code, not JIT from PTX) and the
+ * number of SMs.  Any pointer may be null.  No reference counterpart. */
+gp_status gp_ctx_device_info(const gp_ctx *ctx, int *compute_capability, int *binary_version, int *num_sms);
 
 /* ------------------------------------------------------------------ */
 /* mesh                                                                */
@@ -226,21 +231,27 @@ gp_status gp_ctx_step_trace(gp_ctx *ctx, uint32_t cap, uint64_t *out, uint32_t *
 
 /*
  * gp_toplesets without any device allocation, for callers that may not
- * allocate device memory while they work (an application that gave all device
- * memory to its own pool up front, a latency-critical loop where cudaMalloc /
- * cudaFree, which can stall the device, are not allowed).  No reference
- * counterpart: it is che::compute_toplesets' result (src/che.cpp:546-593)
- * computed into caller-provided DEVICE buffers.
+ * allocate device memory while they work: an application that handed all
+ * device memory to its own pool up front, or a latency-critical loop in which
+ * cudaMalloc / cudaFree (which can stall the whole device) are not allowed.
+ * It has no counterpart in the reference: the results are gp_toplesets' (the
+ * toplesets rings, sorted order and limits), written to caller-provided
+ * DEVICE buffers.
  *
  * The BFS scratch (8 bytes per vertex plus a 4 KiB descriptor) is a fixed
  * array inside the library, about 8 MiB, reserved on every GPU that loads the
  * library until the process exits; meshes above 2^20 vertices get
- * GP_ERR_CAPACITY.  The mesh's device must be current.  The first call on a
- * device looks up the array's device address (cudaGetSymbolAddress); make that
- * first call before any stream capture.  Work is enqueued on `stream` (a
- * cudaStream_t, 0 = default stream) and the call returns without waiting.
- * All calls share the one array: calls that overlap on the GPU (other streams,
- * other threads) race and must be serialised by the caller.
+ * GP_ERR_CAPACITY.  The mesh's device must be current.  Every call made
+ * outside stream capture looks up the array's device address
+ * (cudaGetSymbolAddress), so a device reset between calls is harmless; a call
+ * made while its stream is being captured reuses the address found by the
+ * last uncaptured call on that device, so the first call on a device (and the
+ * first after a device reset) must come before any capture, else the call
+ * returns GP_ERR_INVALID_ARG.  Work is enqueued on `stream` (a cudaStream_t,
+ * 0 = default stream) and the call returns without waiting.  All calls share
+ * the one array, which keeps the last call's contents (each call clears what
+ * must start at zero): calls that overlap on the GPU (other streams, other
+ * threads) race and must be serialised by the caller.
  *
  * sources: device array of n_sources vertex ids.  rings[n_vertices],
  * sorted[cap_sorted >= n_vertices + n_sources], limits[cap_limits >=

@@ -21,6 +21,14 @@ def dev_mesh(ctx, xyz, tri):
     return _capi.DeviceMesh(ctx, xyz, tri)
 
 
+def test_loaded_code_is_native_sm103(gpu_ctx):
+    """The kernels run from native sm_103 code built by build(), not from PTX
+    JIT-compiled by the driver: the binary version of the loaded sweep kernel
+    (cudaFuncGetAttributes) is 103 on a compute capability 10.3 device."""
+    cc, bv, n_sm = gpu_ctx.device_info()
+    assert cc == 103 and bv == 103 and n_sm > 0
+
+
 @pytest.mark.parametrize("name,g", CASES, ids=[c[0] for c in CASES])
 def test_toplesets_bit_exact_golden(gpu_ctx, name, g):
     from gproshan_gb300 import _capi
