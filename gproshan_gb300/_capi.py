@@ -45,7 +45,8 @@ class gp_ptp_opts(C.Structure):
     _fields_ = [("precision", C.c_uint32), ("max_iter", C.c_uint32), ("tol", C.c_double),
                 ("threads", C.c_uint32), ("ctas", C.c_uint32), ("local_window", C.c_uint32),
                 ("round_coords", C.c_uint32), ("schedule", C.c_uint32), ("grid_kernel", C.c_uint32),
-                ("queue_min", C.c_uint32), ("queue_tile", C.c_uint32)]
+                ("queue_min", C.c_uint32), ("queue_tile", C.c_uint32), ("normalize", C.c_uint32),
+                ("reserved2", C.c_uint32)]
 
 
 class gp_ptp_stats(C.Structure):
@@ -79,6 +80,7 @@ SIGNATURES = {
     "gp_status_str": (C.c_char_p, [C.c_int]),
     "gp_ctx_stream": (C.c_void_p, [C.c_void_p]),
     "gp_ctx_workspace_bytes": (C.c_size_t, [C.c_void_p]),
+    "gp_ctx_valid": (C.c_int, [C.c_void_p]),
     "gp_ctx_device_info": (C.c_int, [C.c_void_p, C.POINTER(C.c_int), C.POINTER(C.c_int), C.POINTER(C.c_int)]),
     "gp_che_build": (C.c_int, [C.c_uint32, C.c_uint32, C.c_void_p, C.c_void_p, C.c_void_p,
                                C.POINTER(C.c_int)]),
@@ -348,8 +350,10 @@ GP_GRID_QUEUE = 2
 
 def make_opts(precision: int = GP_F32, max_iter: int = 0, tol: float = 0.0, ctas: int = 0,
               local_window: int = 0, round_coords: bool = False, schedule: int = GP_SCHED_REACTIVE,
-              grid_kernel: int = GP_GRID_AUTO, queue_min: int = 0, queue_tile: int = 0) -> gp_ptp_opts:
+              grid_kernel: int = GP_GRID_AUTO, queue_min: int = 0, queue_tile: int = 0,
+              normalize: bool = False) -> gp_ptp_opts:
     o = gp_ptp_opts()
+    o.normalize = int(bool(normalize))
     o.queue_tile = queue_tile
     o.schedule = schedule
     o.grid_kernel = grid_kernel

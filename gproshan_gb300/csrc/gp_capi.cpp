@@ -3,7 +3,10 @@
 //   toplesets (BFS) -> ring renumbering -> persistent sweeps -> gather.
 #include <algorithm>
 #include <cmath>
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cstdarg>
+#include <mutex>
 #include <cstdio>
 #include <cstring>
 #include <string>
@@ -24,8 +27,13 @@ cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uin
                                   uint32_t total, uint32_t *cnt, uint32_t *scan_tmp, bool f64, bool clusters,
                                   cudaStream_t s);
 cudaError_t launch_gather_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
-                                uint32_t total, bool f64, bool clusters, cudaStream_t s);
+                                uint32_t total, bool f64, bool clusters, cudaStream_t s, unsigned long long *amax = nullptr, bool nmax = false);
+cudaError_t launch_normalize_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
+                                   uint32_t total, bool out_f64, cudaStream_t s);
 cudaError_t launch_normalize(void *dist, bool f64, uint64_t n, unsigned long long *tmp, cudaStream_t s);
+cudaError_t launch_fps_sources(FieldDev *field, const FpsDev *c, cudaStream_t s);
+cudaError_t launch_fps_append(const void *dist, bool f64, uint32_t n, FpsDev *c, uint32_t *samples, double radio,
+                              const FpsErr &e, cudaStream_t s);
 int ptp_local_max_ctas(int device, bool f64, bool clusters);
 cudaError_t launch_classify(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t local_window,
                             const uint32_t *pred_big, cudaStream_t s);
@@ -60,6 +68,7 @@ struct gp_ctx {
 	size_t pin_bytes = 0;
 	cudaEvent_t ev0 = nullptr, ev1 = nullptr;
 	cudaEvent_t ph[6] = {};    // phase boundaries of the last call
+	cudaEvent_t fps0 = nullptr, fps1 = nullptr;  // start / end of a farthest-point sampling loop
 	gp_call_stats last{};
 	unsigned long long *steps = nullptr;   // grid-launch step trace (device), if enabled
 	uint32_t steps_cap = 0;
@@ -72,10 +81,13 @@ struct gp_ctx {
 	float *model = nullptr;    // cost-model parameters (device), or null
 	uint32_t dbg_spin = 0;     // grid-barrier poll limit (0: the default)
 	uint32_t dbg_phantom = 0;  // extra arrivals the grid barrier waits for (tests of the bounded wait)
+	unsigned long long cu_id = 0;  // id of the CUDA context the handles above belong to (0: unknown)
 };
 
 struct gp_mesh {
 	gp_ctx *ctx = nullptr;
+	int device = 0;
+	unsigned long long cu_id = 0;  // CUDA context the block was allocated in (0: unknown)
 	uint32_t nv = 0, nf = 0;
 	MeshDev dev{};
 	void *block = nullptr;     // one device allocation holding the mesh arrays
@@ -216,6 +228,18 @@ struct TopOut {  // host outputs of gp_toplesets
 	uint32_t *n_limits;
 };
 
+// A farthest-point sampling loop run by one call of run(): up to n_iter
+// samples appended to the device copy of samples[0, n_init), with no host
+// round trip per sample (see fps_append_kernel).
+struct FpsLoop {
+	uint32_t *samples;    // host: n_init seeds in, the appended samples out (capacity n_init + n_iter)
+	uint32_t n_init;
+	uint32_t n_iter;      // samples to take at most
+	double radio;         // stop once the farthest distance is <= radio
+	uint32_t n_out;       // out: samples in total
+	double max_dist;      // out: farthest distance of the last sample's field
+};
+
 gp_status map_dev_err(gp_ctx *ctx, uint32_t err, const char *where)
 {
 	if(!err) return GP_OK;
@@ -230,8 +254,9 @@ gp_status map_dev_err(gp_ctx *ctx, uint32_t err, const char *where)
 
 gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts, gp_dtype out_type,
               bool src_dev, bool out_dev, Stage stage, const TopOut *top, double *seconds, float *features = nullptr,
-              gp_plan *plan = nullptr)
+              gp_plan *plan = nullptr, FpsLoop *fps = nullptr)
 {
+	if(fps && (F != 1 || stage != Stage::ptp || plan || src_dev || out_dev || reqs[0].clusters)) return GP_ERR_INVALID_ARG;
 	if(!ctx) return GP_ERR_INVALID_ARG;
 	if(!F) return GP_OK;
 	const gp_ptp_opts o = opts ? *opts : gp_ptp_opts{};
@@ -264,7 +289,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		}
 		const uint32_t nv = r.mesh->nv;
 		if(!src_dev)
-			for(uint32_t s = 0; s < r.ns; s++)
+			for(uint32_t s = 0; s < (fps ? fps->n_init : r.ns); s++)
 				if(r.src[s] >= nv)
 				{
 					set_err(ctx, "field %u: source %u = %u out of range (n_vertices %u)", f, s, r.src[s], nv);
@@ -355,6 +380,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		if(!out_dev) o_out = cv.add<char>(vtot * osz);
 	}
 	const size_t o_src = cv.add<uint32_t>(stot);
+	const size_t o_fps = fps ? cv.add<FpsDev>(1) : 0;
 	gp_status st = GP_OK;
 	if(plan)
 	{
@@ -379,7 +405,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		FieldDev &d = hf[f];
 		std::memset(&d, 0, sizeof(d));
 		d.m = r.mesh->dev;
-		d.ns = r.ns;
+		d.ns = fps ? fps->n_init : r.ns;  // an FPS field's count grows on the device (capacity r.ns)
 		d.cap_sorted = r.mesh->nv + r.ns;
 		d.src = src_dev ? r.src : reinterpret_cast<const uint32_t *>(P(o_src)) + sbase[f];
 		d.ring = reinterpret_cast<uint32_t *>(P(o_ring)) + base[f];
@@ -441,7 +467,17 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	GP_CUDA(ctx, stage_copy(o_base, base.data(), 4 * (F + 1)));
 	GP_CUDA(ctx, stage_copy(o_vbase, vbase.data(), 4 * (F + 1)));
 	if(!wide.empty()) GP_CUDA(ctx, stage_copy(o_wide, wide.data(), 4 * wide.size()));
-	if(!src_dev)
+	if(fps)
+	{
+		// the seeds; the field's source count starts at n_init and grows on the device
+		GP_CUDA(ctx, stage_copy(o_src, reqs[0].src, 4 * (size_t) fps->n_init));
+		FpsDev fd{};
+		fd.ns = fps->n_init;
+		fd.ns_max = reqs[0].ns;
+		fd.max_dist = INFINITY;
+		GP_CUDA(ctx, stage_copy(o_fps, &fd, sizeof(fd)));
+	}
+	else if(!src_dev)
 	{
 		std::vector<uint32_t> all(stot);
 		for(uint32_t f = 0; f < F; f++) std::memcpy(all.data() + sbase[f], reqs[f].src, 4 * (size_t) reqs[f].ns);
@@ -489,7 +525,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	cs.n_fields = F;
 	auto record = [&](cudaEvent_t ev) { return plan ? cudaSuccess : cudaEventRecord(ev, s); };
 	auto device_work = [&]() -> gp_status {
-	if(plan) GP_CUDA(ctx, cudaMemsetAsync(dS, 0, sizeof(FieldState) * F, s));
+	if(plan || fps) GP_CUDA(ctx, cudaMemsetAsync(dS, 0, sizeof(FieldState) * F, s));
 	GP_CUDA(ctx, cudaMemsetAsync(dSync, 0, 2 * sizeof(GridSync), s));
 	GP_CUDA(ctx, record(ctx->ev0));
 	GP_CUDA(ctx, record(ctx->ph[0]));
@@ -551,7 +587,14 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		                        reinterpret_cast<uint32_t *>(P(o_bar)), ctas, f64, clusters, ctx->steps,
 		                        ctx->steps_cap, dctl, ctx->dbg_spin, ctx->dbg_phantom, s));
 		GP_CUDA(ctx, record(ctx->ph[4]));
-		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s));
+		FpsDev *dfps = fps ? reinterpret_cast<FpsDev *>(P(o_fps)) : nullptr;
+		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s,
+		                                 dfps ? &dfps->amax : nullptr, o.normalize != 0));
+		if(o.normalize)
+		{
+			GP_CUDA(ctx, launch_normalize_batch(dF, dS, dBase, F, (uint32_t) tot, out_type == GP_F64, s));
+			cs.launches += 1;
+		}
 		cs.launches += 6;
 	}
 	else
@@ -581,18 +624,67 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		GP_CUDA(ctx, cudaGraphInstantiate(&plan->exec, g, 0));
 		return GP_OK;
 	}
-	st = device_work();
-	if(st != GP_OK) return st;
+	if(fps)
+	{
+		// farthest-point sampling: every sample's work enqueued back to back;
+		// with a radius the host looks at the device's stop flag every 8
+		// samples, else only at the end
+		FpsDev *dfps = reinterpret_cast<FpsDev *>(P(o_fps));
+		uint32_t *dsamp = reinterpret_cast<uint32_t *>(P(o_src));
+		const FpsErr fe{dSync, reinterpret_cast<const uint32_t *>(P(o_bar)),
+		                reinterpret_cast<const QCtl *>(P(o_qctl)), dS,
+		                wide.empty() ? nullptr : reinterpret_cast<const uint32_t *>(P(o_wbar))};
+		const uint32_t chunk = fps->radio > 0 ? 8u : std::max(fps->n_iter, 1u);
+		GP_CUDA(ctx, cudaEventRecord(ctx->fps0, s));
+		for(uint32_t it = 0; it < fps->n_iter;)
+		{
+			const uint32_t n = std::min(chunk, fps->n_iter - it);
+			for(uint32_t k = 0; k < n; k++)
+			{
+				GP_CUDA(ctx, launch_fps_sources(dF, dfps, s));
+				st = device_work();
+				if(st != GP_OK) return st;
+				GP_CUDA(ctx, launch_fps_append(hf[0].dist_out, out_type == GP_F64, reqs[0].mesh->nv, dfps, dsamp,
+				                               fps->radio, fe, s));
+			}
+			it += n;
+			if(it < fps->n_iter)
+			{
+				uint32_t stop = 0;
+				GP_CUDA(ctx, cudaMemcpyAsync(&stop, &dfps->stop, 4, cudaMemcpyDeviceToHost, s));
+				GP_CUDA(ctx, cudaStreamSynchronize(s));
+				if(stop) break;
+			}
+		}
+		GP_CUDA(ctx, cudaEventRecord(ctx->fps1, s));
+	}
+	else
+	{
+		st = device_work();
+		if(st != GP_OK) return st;
+	}
 
 	// ---- downloads -------------------------------------------------------------
 	GridSync hsync[2];
 	GP_CUDA(ctx, cudaMemcpyAsync(hsync, dSync, sizeof(hsync), cudaMemcpyDeviceToHost, s));
 	GP_CUDA(ctx, cudaMemcpyAsync(hs.data(), dS, sizeof(FieldState) * F, cudaMemcpyDeviceToHost, s));
 	d2h += sizeof(hsync) + sizeof(FieldState) * F;
-	if(stage == Stage::ptp && !out_dev)
+	if(stage == Stage::ptp && !out_dev && !fps)
 		for(uint32_t f = 0; f < F; f++)
 			d2h += (uint64_t) reqs[f].mesh->nv * (osz + (reqs[f].clusters ? 4 : 0));
-	if(stage == Stage::ptp && !out_dev)
+	FpsDev hfps{};
+	if(fps)
+	{
+		GP_CUDA(ctx, cudaMemcpyAsync(&hfps, P(o_fps), sizeof(hfps), cudaMemcpyDeviceToHost, s));
+		GP_CUDA(ctx, cudaStreamSynchronize(s));
+		if(hfps.ns > fps->n_init)
+			GP_CUDA(ctx, cudaMemcpyAsync(fps->samples + fps->n_init, reinterpret_cast<uint32_t *>(P(o_src)) + fps->n_init,
+			                             4 * (size_t) (hfps.ns - fps->n_init), cudaMemcpyDeviceToHost, s));
+		d2h += sizeof(hfps) + 4 * (size_t) (hfps.ns - fps->n_init);
+		fps->n_out = hfps.ns;
+		fps->max_dist = hfps.max_dist;
+	}
+	if(stage == Stage::ptp && !out_dev && !fps)
 		for(uint32_t f = 0; f < F; f++)
 		{
 			const size_t nv = reqs[f].mesh->nv;
@@ -619,10 +711,10 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		GP_CUDA(ctx, cudaMemcpy(wb, P(o_wbar), sizeof(wb), cudaMemcpyDeviceToHost));
 		ferr |= wb[2];
 	}
-	st = map_dev_err(ctx, hsync[0].err | hsync[1].err | ferr, stage == Stage::ptp ? "ptp" : "toplesets");
+	st = map_dev_err(ctx, hsync[0].err | hsync[1].err | ferr | hfps.err, stage == Stage::ptp ? "ptp" : "toplesets");
 	if(st != GP_OK) return st;
 	float ms = 0.f;
-	GP_CUDA(ctx, cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1));
+	GP_CUDA(ctx, cudaEventElapsedTime(&ms, fps ? ctx->fps0 : ctx->ev0, fps ? ctx->fps1 : ctx->ev1));
 	if(seconds) *seconds = ms * 1e-3;
 	{
 		float pm[5];
@@ -712,6 +804,54 @@ const char *gp_status_str(gp_status s)
 	return "unknown status";
 }
 
+namespace gp {
+namespace {
+
+// Unique id of the calling thread's current CUDA context (cuCtxGetId), or 0
+// when it cannot be told.  The driver functions are found through the runtime
+// (no link against the driver library).  A device reset destroys the primary
+// context; the next runtime call makes a new one with a new id.
+unsigned long long current_ctx_id()
+{
+	static PFN_cuCtxGetCurrent_v4000 get_cur = nullptr;
+	static PFN_cuCtxGetId_v12000 get_id = nullptr;
+	static std::once_flag once;
+	std::call_once(once, [] {
+		cudaDriverEntryPointQueryResult q{};
+		void *p = nullptr;
+		if(cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 4000, cudaEnableDefault, &q) == cudaSuccess &&
+		   q == cudaDriverEntryPointSuccess)
+			get_cur = reinterpret_cast<PFN_cuCtxGetCurrent_v4000>(p);
+		p = nullptr;
+		if(cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+		   q == cudaDriverEntryPointSuccess)
+			get_id = reinterpret_cast<PFN_cuCtxGetId_v12000>(p);
+		cudaGetLastError();
+	});
+	if(!get_cur || !get_id) return 0;
+	CUcontext c = nullptr;
+	unsigned long long id = 0;
+	if(get_cur(&c) != CUDA_SUCCESS || !c || get_id(c, &id) != CUDA_SUCCESS) return 0;
+	return id;
+}
+
+// ctx's handles still belong to its device's current context (no device reset since)
+bool ctx_alive(const gp_ctx *ctx)
+{
+	if(cudaSetDevice(ctx->device) != cudaSuccess)
+	{
+		cudaGetLastError();
+		return false;
+	}
+	const unsigned long long id = current_ctx_id();
+	return !id || !ctx->cu_id || id == ctx->cu_id;
+}
+
+} // namespace
+} // namespace gp
+
+int gp_ctx_valid(const gp_ctx *ctx) { return ctx && ctx_alive(ctx) ? 1 : 0; }
+
 gp_status gp_ctx_create(int device, gp_ctx **out)
 {
 	if(!out) return GP_ERR_INVALID_ARG;
@@ -736,6 +876,7 @@ gp_status gp_ctx_create(int device, gp_ctx **out)
 		return GP_ERR_CUDA;
 	}
 	cudaDeviceGetAttribute(&ctx->num_sms, cudaDevAttrMultiProcessorCount, device);
+	ctx->cu_id = current_ctx_id();
 	ctx->bfs_ctas = toplesets_max_ctas(device);
 	ctx->bfs_wide_ctas = toplesets_wide_ctas(device);
 	for(int k = 0; k < 4; k++)
@@ -746,6 +887,7 @@ gp_status gp_ctx_create(int device, gp_ctx **out)
 	}
 	for(int k = 0; k < 6; k++)
 		if(cudaEventCreate(&ctx->ph[k]) != cudaSuccess) ctx->ph[k] = nullptr;
+	if(cudaEventCreate(&ctx->fps0) != cudaSuccess || cudaEventCreate(&ctx->fps1) != cudaSuccess) ctx->ph[5] = nullptr;
 	if(ctx->bfs_ctas <= 0 || ctx->ptp_ctas[0] <= 0 || !ctx->ph[5])
 	{
 		cudaGetLastError();
@@ -759,7 +901,12 @@ gp_status gp_ctx_create(int device, gp_ctx **out)
 void gp_ctx_destroy(gp_ctx *ctx)
 {
 	if(!ctx) return;
-	cudaSetDevice(ctx->device);
+	if(!ctx_alive(ctx))
+	{
+		// the device was reset: its handles died with the old context
+		delete ctx;
+		return;
+	}
 	if(ctx->stream) cudaStreamSynchronize(ctx->stream);
 	if(ctx->ws) cudaFree(ctx->ws);
 	if(ctx->pin) cudaFreeHost(ctx->pin);
@@ -769,6 +916,8 @@ void gp_ctx_destroy(gp_ctx *ctx)
 	if(ctx->ev1) cudaEventDestroy(ctx->ev1);
 	for(int k = 0; k < 6; k++)
 		if(ctx->ph[k]) cudaEventDestroy(ctx->ph[k]);
+	if(ctx->fps0) cudaEventDestroy(ctx->fps0);
+	if(ctx->fps1) cudaEventDestroy(ctx->fps1);
 	if(ctx->stream) cudaStreamDestroy(ctx->stream);
 	delete ctx;
 }
@@ -1059,6 +1208,8 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 	}
 	gp_mesh *m = new gp_mesh;
 	m->ctx = ctx;
+	m->device = ctx->device;
+	m->cu_id = ctx->cu_id;
 	m->nv = nv;
 	m->nf = nf;
 	Carve mc;
@@ -1117,10 +1268,22 @@ gp_status gp_mesh_create(gp_ctx *ctx, uint32_t nv, const double *xyz, uint32_t n
 
 void gp_mesh_destroy(gp_mesh *m)
 {
-	// cudaFree waits for work on the buffer; the owning context is not
-	// touched, so meshes may outlive (and be freed after) their context.
+	// cudaFree waits for work on the buffer; the owning gp_ctx is not
+	// touched, so meshes may outlive (and be freed after) their context.  A
+	// block that died with a device reset is not freed again.
 	if(!m) return;
-	if(m->block) cudaFree(m->block);
+	if(m->block)
+	{
+		int prev = -1;
+		cudaGetDevice(&prev);
+		if(cudaSetDevice(m->device) == cudaSuccess)
+		{
+			const unsigned long long id = current_ctx_id();
+			if(!id || !m->cu_id || id == m->cu_id) cudaFree(m->block);
+		}
+		if(prev >= 0) cudaSetDevice(prev);
+		cudaGetLastError();
+	}
 	delete m;
 }
 
@@ -1449,50 +1612,27 @@ gp_status gp_fps(gp_ctx *ctx, gp_mesh *mesh, uint32_t *samples, uint32_t n_init,
 	// farthest_point_sampling_ptp_gpu (src/cuda/geodesics_ptp.cu:122-147)
 	if(n >= mesh->nv) n = mesh->nv >> 1;
 	n = n > n_init ? n - n_init : 0;  // the reference underflows when n < |samples|
-	uint32_t ns = n_init;
-	double md = INFINITY, total = 0;
-	std::vector<float> df;
-	std::vector<double> dd;
+	n = std::min<uint64_t>(n, cap - n_init);
+	*n_out = n_init;
+	*max_dist = INFINITY;
+	if(seconds) *seconds = 0;
+	if(!n) return GP_OK;
 	const bool f64 = opts && opts->precision == GP_F64;
-	// distances stay on the device: a device buffer from the workspace tail is
-	// not possible (run() reuses it), so use a dedicated allocation
-	void *ddist = nullptr;
-	unsigned long long *dmax = nullptr;
-	GP_CUDA(ctx, cudaMalloc(&ddist, (size_t) mesh->nv * (f64 ? 8 : 4)));
-	cudaError_t e0 = cudaMalloc(&dmax, 16);
-	if(e0 != cudaSuccess)
-	{
-		cudaFree(ddist);
-		set_err(ctx, "cudaMalloc: %s", cudaGetErrorString(e0));
-		return GP_ERR_OUT_OF_MEMORY;
-	}
-	gp_status st = GP_OK;
-	while(n-- && md > radio && ns < cap)
-	{
-		Req r{mesh, samples, ns, nullptr, 0, nullptr, ddist, nullptr, nullptr};
-		double sec = 0;
-		// sources are host values; outputs stay on the device
-		st = run(ctx, &r, 1, opts, f64 ? GP_F64 : GP_F32, false, true, Stage::ptp, nullptr, &sec);
-		if(st != GP_OK) break;
-		total += sec;
-		unsigned long long h[2];
-		if(launch_argmax_abs(ddist, f64, mesh->nv, dmax, ctx->stream) != cudaSuccess ||
-		   cudaMemcpyAsync(h, dmax, 16, cudaMemcpyDeviceToHost, ctx->stream) != cudaSuccess ||
-		   cudaStreamSynchronize(ctx->stream) != cudaSuccess)
-		{
-			set_err(ctx, "fps argmax failed");
-			st = GP_ERR_CUDA;
-			break;
-		}
-		const uint32_t fidx = (uint32_t) h[1];
-		if(radio > 0 || !n) std::memcpy(&md, &h[0], sizeof(double));
-		samples[ns++] = fidx;
-	}
-	cudaFree(ddist);
-	cudaFree(dmax);
-	*n_out = ns;
-	*max_dist = md;
-	if(seconds) *seconds = total;
+	// one call: layout and uploads once, then every sample's device work back
+	// to back (sources, outputs and the argmax stay on the device); the
+	// workspace is the context's, so nothing is allocated per call once it has
+	// grown to this size
+	FpsLoop loop{samples, n_init, (uint32_t) n, radio, n_init, (double) INFINITY};
+	std::vector<char> scratch;  // the field's output is never read back
+	Req r{mesh, samples, (uint32_t) (n_init + n), nullptr, 0, nullptr, nullptr, nullptr, nullptr};
+	scratch.resize(1);
+	r.dist = scratch.data();
+	double sec = 0;
+	const gp_status st = run(ctx, &r, 1, opts, f64 ? GP_F64 : GP_F32, false, false, Stage::ptp, nullptr, &sec, nullptr,
+	                         nullptr, &loop);
+	*n_out = loop.n_out;
+	*max_dist = loop.max_dist;
+	if(seconds) *seconds = sec;
 	return st;
 }
 

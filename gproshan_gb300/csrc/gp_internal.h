@@ -127,6 +127,16 @@ struct FieldDev {
 	float tol32;              // tol rounded to float (the FP32 path's ring test)
 };
 
+// Device-side state of a farthest-point sampling loop (gp_fps).
+struct FpsDev {
+	uint32_t ns;                // samples so far (the field's source count)
+	uint32_t ns_max;            // capacity of the sample array
+	uint32_t stop;              // the loop has ended (radius reached, array full, or a device error)
+	uint32_t err;               // DEV_ERR_* bits seen by any sample
+	double max_dist;            // max |d| of the last sample's field
+	unsigned long long amax;    // max |d| bits of the current field (gather), reset by the append
+};
+
 // Mutable per-field state of the persistent launches.
 struct FieldState {
 	// toplesets
@@ -138,8 +148,18 @@ struct FieldState {
 	uint32_t win_s, win_e, chk_e, nr;  // current window, check-ring end, reached vertices
 	uint32_t big;        // 1: swept by the grid-wide launch, 0: by one CTA
 	unsigned long long relax;
+	unsigned long long nmax;  // largest finite positive output (bits), for gp_ptp_opts::normalize
 };
 
+
+// Where a sample's device errors are (all cleared before each sample runs).
+struct FpsErr {
+	const GridSync *sync;       // 2: BFS / sweep barrier words
+	const uint32_t *bar;        // lockstep barrier block ([2] = error bits)
+	const QCtl *ctl;            // work-queue control
+	const FieldState *state;    // the field's state (status)
+	const uint32_t *wbar;       // whole-GPU BFS barrier block, or null
+};
 
 // ------------------------------------------------------------------
 // Kernel entry points implemented in the .cu files (all asynchronous on `s`).
@@ -170,8 +190,6 @@ cudaError_t launch_toplesets_wide(FieldDev *fields, FieldState *state, const uin
 
 // gp_ptp.cu
 int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields);
-cudaError_t launch_argmax_abs(const void *dist, bool f64, uint32_t n, unsigned long long *out,
-                              cudaStream_t s);
 
 // gp_mesh.cu: sums for the geometry statistics (8 doubles, zeroed by the caller):
 // [0] sum l, [1] sum l^2, [2] sum log l, [3] sum (log l)^2, [4] edges,

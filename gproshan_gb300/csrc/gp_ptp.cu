@@ -1375,6 +1375,8 @@ struct CatArgs {
 	uint32_t n_fields;
 	uint32_t total;
 	uint32_t *cnt;         // total (+1) counts, then global fan offsets after the scan
+	unsigned long long *amax = nullptr;  // gather only: null, or max |out| (bits) of the call, atomicMax'ed
+	bool nmax = false;                   // gather only: reduce each field's largest finite output into state.nmax
 };
 
 __global__ void inv_clear_kernel(CatArgs c)
@@ -1526,6 +1528,7 @@ __global__ void fill_kernel(CatArgs c)
 template <typename T, bool CL>
 __global__ void gather_kernel(CatArgs c)
 {
+	unsigned long long mloc = 0;
 	for(uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < c.total; g += gridDim.x * blockDim.x)
 	{
 		const uint32_t f = upper_index(c.base, c.n_fields, g);
@@ -1542,15 +1545,100 @@ __global__ void gather_kernel(CatArgs c)
 			x = (double) h.x + (double) h.y;
 		}
 		else x = static_cast<const double *>(F.D[st.d])[k];
-		if(F.out_f64) static_cast<double *>(F.dist_out)[v] = x;
-		else static_cast<float *>(F.dist_out)[v] = (float) x;
+		double y;
+		if(F.out_f64) static_cast<double *>(F.dist_out)[v] = y = x;
+		else static_cast<float *>(F.dist_out)[v] = (float) x, y = (double) (float) x;
 		if(CL && F.clusters_out)
 			F.clusters_out[v] = iv ? F.C[st.d][k] : (F.clusters_in ? F.clusters_in[v] : 0u);
+		// farthest-point sampling: max |out| over the call (the value cublasI?amax
+		// looks for, src/cuda/geodesics_ptp.cu:138-142), fused into the gather
+		if(c.amax) mloc = max(mloc, (unsigned long long) __double_as_longlong(fabs(y)));
+		if(c.nmax)
+		{
+			// normalize_ptp's maximum over dist[v] < INFINITY (distances are >= 0,
+			// so the bit patterns order like the values): lanes of one field
+			// reduce together, 32-bit halves at a time, and one of them adds it
+			const unsigned long long b = y < INFINITY && y > 0 ? (unsigned long long) __double_as_longlong(y) : 0ull;
+			const unsigned grp = __match_any_sync(__activemask(), f);
+			const uint32_t hi = __reduce_max_sync(grp, (uint32_t) (b >> 32));
+			const uint32_t lo = __reduce_max_sync(grp, (uint32_t) (b >> 32) == hi ? (uint32_t) b : 0u);
+			if((threadIdx.x & 31) == (uint32_t) (__ffs(grp) - 1) && hi)
+				atomicMax(&c.state[f].nmax, ((unsigned long long) hi << 32) | lo);
+		}
+	}
+	if(c.amax)
+	{
+		for(int o = 16; o; o >>= 1) mloc = max(mloc, __shfl_xor_sync(0xffffffffu, mloc, o));
+		if((threadIdx.x & 31) == 0 && mloc) atomicMax(c.amax, mloc);
+	}
+}
+
+// normalize_ptp (src/geodesics_ptp.cpp:264-276) of every field's output, on
+// the maximum the gather reduced: dist[v] /= max_d.
+template <typename O>
+__global__ void normalize_batch_kernel(CatArgs c)
+{
+	for(uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < c.total; g += gridDim.x * blockDim.x)
+	{
+		const uint32_t f = upper_index(c.base, c.n_fields, g);
+		const uint32_t v = g - c.base[f];
+		const FieldDev &F = c.fields[f];
+		if(v >= F.m.nv) continue;
+		const O m = (O) __longlong_as_double((long long) c.state[f].nmax);
+		static_cast<O *>(F.dist_out)[v] /= m;
 	}
 }
 
 // ---------------------------------------------------------------------------
-// normalize_ptp and argmax |x|
+// Farthest-point sampling on the device (farthest_point_sampling_ptp_gpu,
+// src/cuda/geodesics_ptp.cu:122-147): the sample loop runs without a host
+// round trip.  Per sample: fps_sources_kernel sets the field's source count
+// from the device counter, the usual BFS / renumbering / sweeps / gather run
+// (the gather also reduces max |d|), and fps_append_kernel appends the first
+// vertex holding that maximum (cublasI?amax's pick, 0-based) and applies the
+// loop's stop rule.  Once stopped, later samples change nothing.
+// ---------------------------------------------------------------------------
+__global__ void fps_sources_kernel(FieldDev *field, const FpsDev *c)
+{
+	if(threadIdx.x == 0) field->ns = c->ns;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(1024) fps_append_kernel(const T *x, uint32_t n, FpsDev *c, uint32_t *samples,
+                                                          double radio, FpsErr e)
+{
+	__shared__ uint32_t s_min;
+	if(threadIdx.x == 0) s_min = 0xFFFFFFFFu;
+	__syncthreads();
+	const unsigned long long m = c->amax;
+	for(uint32_t base = 0; base < n; base += blockDim.x)
+	{
+		const uint32_t i = base + threadIdx.x;
+		if(i < n && (unsigned long long) __double_as_longlong(fabs((double) x[i])) == m) atomicMin(&s_min, i);
+		if(__syncthreads_or(s_min != 0xFFFFFFFFu)) break;
+	}
+	if(threadIdx.x != 0) return;
+	c->amax = 0;  // for the next sample
+	// this sample's device errors (they are cleared before the next sample runs)
+	uint32_t err = e.sync[0].err | e.sync[1].err | e.bar[2] | e.ctl->err | e.state->status;
+	if(e.wbar) err |= e.wbar[2];
+	if(err)
+	{
+		c->err |= err;
+		c->stop = 1;
+	}
+	if(c->stop || s_min == 0xFFFFFFFFu) return;
+	samples[c->ns] = s_min;
+	c->ns++;
+	const double md = __longlong_as_double((long long) m);
+	c->max_dist = md;
+	// while(n-- && max_dist > radio): with a radius the loop ends once it is
+	// reached (without one the reference never reads max_dist before the end)
+	if((radio > 0 && !(md > radio)) || c->ns >= c->ns_max) c->stop = 1;
+}
+
+// ---------------------------------------------------------------------------
+// normalize_ptp of a caller array (gp_normalize_ptp)
 // ---------------------------------------------------------------------------
 template <typename T>
 __global__ void max_finite_kernel(const T *x, uint64_t n, unsigned long long *out)
@@ -1571,27 +1659,6 @@ __global__ void divide_kernel(T *x, uint64_t n, const unsigned long long *mx)
 	const T m = (T) __longlong_as_double((long long) *mx);
 	for(uint64_t i = blockIdx.x * (uint64_t) blockDim.x + threadIdx.x; i < n; i += (uint64_t) gridDim.x * blockDim.x)
 		x[i] /= m;
-}
-
-template <typename T>
-__global__ void max_abs_kernel(const T *x, uint32_t n, unsigned long long *out)
-{
-	unsigned long long m = 0;
-	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-		m = max(m, (unsigned long long) __double_as_longlong(fabs((double) x[i])));
-	for(int o = 16; o; o >>= 1) m = max(m, __shfl_xor_sync(0xffffffffu, m, o));
-	if((threadIdx.x & 31) == 0) atomicMax(out, m);
-}
-
-template <typename T>
-__global__ void first_index_kernel(const T *x, uint32_t n, unsigned long long *out)
-{
-	const unsigned long long m = out[0];
-	unsigned long long best = ~0ull;
-	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-		if((unsigned long long) __double_as_longlong(fabs((double) x[i])) == m) { best = i; break; }
-	for(int o = 16; o; o >>= 1) best = min(best, __shfl_xor_sync(0xffffffffu, best, o));
-	if((threadIdx.x & 31) == 0 && best != ~0ull) atomicMin(out + 1, best);
 }
 
 unsigned grid_for(uint64_t n)
@@ -1629,10 +1696,35 @@ cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uin
 	return cudaGetLastError();
 }
 
-cudaError_t launch_gather_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
-                                uint32_t total, bool f64, bool clusters, cudaStream_t s)
+cudaError_t launch_fps_sources(FieldDev *field, const FpsDev *c, cudaStream_t s)
+{
+	fps_sources_kernel<<<1, 32, 0, s>>>(field, c);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_fps_append(const void *dist, bool f64, uint32_t n, FpsDev *c, uint32_t *samples, double radio,
+                              const FpsErr &e, cudaStream_t s)
+{
+	if(f64) fps_append_kernel<double><<<1, 1024, 0, s>>>((const double *) dist, n, c, samples, radio, e);
+	else fps_append_kernel<float><<<1, 1024, 0, s>>>((const float *) dist, n, c, samples, radio, e);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_normalize_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
+                                   uint32_t total, bool out_f64, cudaStream_t s)
 {
 	CatArgs c{fields, state, base, n_fields, total, nullptr};
+	const unsigned nb = grid_for(total);
+	if(out_f64) normalize_batch_kernel<double><<<nb, 256, 0, s>>>(c);
+	else normalize_batch_kernel<float><<<nb, 256, 0, s>>>(c);
+	return cudaGetLastError();
+}
+
+cudaError_t launch_gather_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
+                                uint32_t total, bool f64, bool clusters, cudaStream_t s, unsigned long long *amax,
+                                bool nmax)
+{
+	CatArgs c{fields, state, base, n_fields, total, nullptr, amax, nmax};
 	const unsigned nb = grid_for(total);
 	if(f64)
 	{
@@ -1796,26 +1888,6 @@ cudaError_t launch_normalize(void *dist, bool f64, uint64_t n, unsigned long lon
 	{
 		max_finite_kernel<float><<<nb, 256, 0, s>>>((const float *) dist, n, tmp);
 		divide_kernel<float><<<nb, 256, 0, s>>>((float *) dist, n, tmp);
-	}
-	return cudaGetLastError();
-}
-
-// out[0] = bits of max |x|, out[1] = first index holding it (cublasI?amax, 0-based)
-cudaError_t launch_argmax_abs(const void *dist, bool f64, uint32_t n, unsigned long long *out, cudaStream_t s)
-{
-	unsigned long long init[2] = {0ull, ~0ull};
-	cudaError_t e = cudaMemcpyAsync(out, init, sizeof(init), cudaMemcpyHostToDevice, s);
-	if(e != cudaSuccess) return e;
-	const unsigned nb = grid_for(n);
-	if(f64)
-	{
-		max_abs_kernel<double><<<nb, 256, 0, s>>>((const double *) dist, n, out);
-		first_index_kernel<double><<<nb, 256, 0, s>>>((const double *) dist, n, out);
-	}
-	else
-	{
-		max_abs_kernel<float><<<nb, 256, 0, s>>>((const float *) dist, n, out);
-		first_index_kernel<float><<<nb, 256, 0, s>>>((const float *) dist, n, out);
 	}
 	return cudaGetLastError();
 }

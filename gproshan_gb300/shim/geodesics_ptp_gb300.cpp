@@ -7,7 +7,9 @@
 // and the geodesics::PTP_GPU dispatch (src/geodesics.cpp:225-240) unchanged.
 // Differences from the reference, all deliberate:
 //   * no cudaDeviceReset (the reference resets the device on every call,
-//     src/cuda/geodesics_ptp.cu:22); one gp_ctx per host thread is kept;
+//     src/cuda/geodesics_ptp.cu:22); one gp_ctx per host thread is kept, and
+//     made again when another part of the application has reset the device
+//     since (gproshan's heat-flow entry points do, src/cuda/heat_flow.cu:47);
 //   * errors are reported (gproshan_error + INFINITY distances) instead of
 //     being ignored;
 //   * distance_t may be double (default build) or float (SINGLE_P): the
@@ -16,6 +18,7 @@
 
 #include "gp_ptp.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <vector>
@@ -30,6 +33,12 @@ gp_ctx *thread_ctx()
 		gp_ctx *ctx = nullptr;
 		~holder() { gp_ctx_destroy(ctx); }
 	} h;
+	if(h.ctx && !gp_ctx_valid(h.ctx))
+	{
+		// the device was reset since: the context's handles are gone
+		gp_ctx_destroy(h.ctx);
+		h.ctx = nullptr;
+	}
 	if(!h.ctx && gp_ctx_create(0, &h.ctx) != GP_OK) h.ctx = nullptr;
 	return h.ctx;
 }
@@ -91,8 +100,24 @@ double parallel_toplesets_propagation_coalescence_gpu(const ptp_out_t &ptp_out, 
                                                       const std::vector<index_t> &sources,
                                                       const toplesets_t &toplesets, const bool &)
 {
-	// this library always sweeps a ring-renumbered copy; same call
-	return run(ptp_out, mesh, sources, toplesets);
+	// The library always sweeps a ring-renumbered copy, so the solve is the
+	// same call.  What differs is the output rule of this entry point
+	// (src/cuda/geodesics_ptp_coalescence.cu:62-86): only the vertices the
+	// toplesets reached (toplesets.index[0, limits.back())) are written; every
+	// other vertex keeps the caller's distance and label.
+	const size_t nv = mesh->n_vertices();
+	const index_t nr = toplesets.limits.empty() ? 0 : toplesets.limits.back();
+	std::vector<distance_t> dist(nv);
+	std::vector<index_t> lab(ptp_out.clusters ? nv : 0);
+	if(ptp_out.clusters) std::copy(ptp_out.clusters, ptp_out.clusters + nv, lab.begin());
+	const double t = run(ptp_out_t(dist.data(), ptp_out.clusters ? lab.data() : nullptr), mesh, sources, toplesets);
+	for(index_t i = 0; i < nr; i++)
+	{
+		const index_t v = toplesets.index[i];
+		ptp_out.dist[v] = dist[v];
+		if(ptp_out.clusters) ptp_out.clusters[v] = lab[v];
+	}
+	return t;
 }
 
 distance_t farthest_point_sampling_ptp_gpu(che *mesh, std::vector<index_t> &samples, double &time_fps, size_t n,

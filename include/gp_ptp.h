@@ -54,6 +54,13 @@ typedef struct gp_mesh gp_mesh;
  * src/cuda/geodesics_ptp.cu:22-46 with a reusable workspace. */
 gp_status gp_ctx_create(int device, gp_ctx **out);
 void gp_ctx_destroy(gp_ctx *ctx);
+/* 1 if the context's device handles are still usable, 0 if the device was
+ * reset since the context was made (cudaDeviceReset destroys the CUDA context
+ * they belong to: gproshan's heat-flow code resets the device on every call,
+ * src/cuda/heat_flow.cu:47).  A dead context can only be destroyed (which then
+ * frees host memory only); meshes made in it are dead too.  No reference
+ * counterpart. */
+int gp_ctx_valid(const gp_ctx *ctx);
 /* Text of the last error seen by this context ("" if none). */
 const char *gp_ctx_last_error(const gp_ctx *ctx);
 const char *gp_status_str(gp_status s);
@@ -125,6 +132,12 @@ typedef struct gp_ptp_opts {
 	                          reach the grid-wide sweeps; 0: default */
 	uint32_t queue_tile;   /* work queue: window vertices per claimed tile (a multiple of
 	                          32, at most 1024); 0: chosen per window */
+	uint32_t normalize;    /* 1: every field's output divided by its largest finite
+	                          distance, as normalize_ptp does (src/geodesics_ptp.cpp:
+	                          264-276; geodesics::normalize, src/geodesics.cpp:78-90),
+	                          on the device before any copy out: the maximum is
+	                          reduced inside the output gather */
+	uint32_t reserved2;
 } gp_ptp_opts;
 
 /* Grid-wide sweeps of the fields that outgrow one CTA.  LOCKSTEP: one

@@ -278,6 +278,57 @@ def test_fps_matches_oracle(gpu_ctx, oracle_lib):
     assert np.array_equal(s, s_ref) and md == md_ref
 
 
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_normalize_option_in_the_call(gpu_ctx, oracle_lib, precision):
+    """gp_ptp_opts.normalize divides every field's output by its largest finite
+    distance on the device (the maximum reduced in the output gather): bit for
+    bit normalize_ptp of the unnormalized output, in a batch with an
+    unreached component (INF stays INF) and fields on several meshes."""
+    from gproshan_gb300 import _capi, meshgen
+    x1, t1 = meshgen.icosphere(3, 0.1, 1)
+    x2, t2 = meshgen.height_field(20, 2)
+    xyz = np.concatenate([x1, x2 + np.array([3.0, 0.0, 0.0])])
+    tri = np.concatenate([t1, t2 + len(x1)]).astype(np.uint32)
+    ms = [dev_mesh(gpu_ctx, xyz, tri), dev_mesh(gpu_ctx, *meshgen.height_field(150, 4))]
+    prec, dt = (_capi.GP_F64, np.float64) if precision == "f64" else (_capi.GP_F32, np.float32)
+    meshes, srcs = [ms[0], ms[1], ms[1]], [[5], [0], [100, 9000]]
+    plain, _, _ = _capi.ptp_batch(gpu_ctx, meshes, srcs, dtype=dt, precision=prec)
+    L = _capi.lib()
+    outs = [np.empty(m.n_vertices, dt) for m in meshes]
+    fields, keep = _capi._fields(meshes, srcs, outs)
+    o = _capi.make_opts(prec, normalize=True)
+    sec = _capi.C.c_double()
+    gpu_ctx.check(L.gp_ptp_batch(gpu_ctx.handle, fields, len(meshes), _capi.C.byref(o),
+                                 _capi.GP_F64 if dt == np.float64 else _capi.GP_F32, 0, _capi.C.byref(sec)), "batch")
+    for a, b in zip(outs, plain):
+        ref = b.copy()
+        m = np.max(ref[np.isfinite(ref)])
+        ref /= dt(m)
+        assert np.array_equal(a, ref)
+        if dt == np.float64:
+            assert np.array_equal(a, oracle_lib.normalize_ptp(b))
+    assert np.isinf(outs[0][len(x1):]).all() and np.max(outs[1]) == 1.0
+
+
+def test_fps_device_loop_matches_oracle_longer_runs(gpu_ctx, oracle_lib):
+    """The device-resident sample loop: 40 samples on a height field and a
+    radius-limited run (the loop stops on the device at the first field whose
+    farthest distance is within the radius), both equal to the oracle's FPS."""
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.height_field(60, 3)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    s_ref, md_ref = oracle_lib.fps(om, 40, [7])
+    s, md, sec = _capi.fps(m, 40, [7], precision=_capi.GP_F64)
+    assert np.array_equal(s, s_ref) and md == md_ref and sec > 0
+    s_ref, md_ref = oracle_lib.fps(om, 200, [7], radio=0.4)
+    s, md, _ = _capi.fps(m, 200, [7], radio=0.4, precision=_capi.GP_F64)
+    assert 1 < len(s_ref) < 200 and np.array_equal(s, s_ref) and md == md_ref
+    # FP32: same samples while the farthest distances are well separated
+    s32, _, _ = _capi.fps(m, 12, [7])
+    assert np.array_equal(s32, oracle_lib.fps(om, 12, [7])[0])
+
+
 def test_normalize_matches_oracle(gpu_ctx, oracle_lib):
     from gproshan_gb300 import _capi
     rng = np.random.default_rng(3)

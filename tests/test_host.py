@@ -99,11 +99,15 @@ def test_cpp_dropin_shim_compiles_against_reference_headers():
         pytest.skip("reference sources (GPROSHAN_REF or the staged copy) or g++ not present")
     ref = os.path.join(src, "include")
     shim = os.path.join(ROOT, "gproshan_gb300", "shim", "geodesics_ptp_gb300.cpp")
-    for extra in ([], ["-DSINGLE_P"]):
-        r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-fopenmp", *extra,
-                            "-I", os.path.join(ROOT, "oracle", "stubs"), "-I", ref,
-                            "-I", os.path.join(ROOT, "include"), shim], capture_output=True, text=True)
-        assert r.returncode == 0, r.stderr
+    driver = os.path.join(ROOT, "tests", "dropin", "dropin_main.cpp")
+    cuda_inc = os.path.join(os.path.dirname(os.path.dirname(shutil.which("nvcc") or "/usr/local/cuda/bin/nvcc")),
+                            "include")
+    for src in (shim, driver):
+        for extra in ([], ["-DSINGLE_P"]):
+            r = subprocess.run(["g++", "-std=c++17", "-fsyntax-only", "-fopenmp", *extra,
+                                "-I", os.path.join(ROOT, "oracle", "stubs"), "-I", ref, "-I", cuda_inc,
+                                "-I", os.path.join(ROOT, "include"), src], capture_output=True, text=True)
+            assert r.returncode == 0, r.stderr
 
 
 def test_ctypes_struct_layouts_match_the_header(tmp_path):
