@@ -261,6 +261,29 @@ def run_gpu(args, rank, world, local):
         # phase times and counts of the same call (the graph carries no events)
         stats = [batched_call() for _ in range(2)]
 
+    # the same batch with the reactive schedule (every field starts on one CTA;
+    # no cost model), otherwise the same options, timed the same way: what the
+    # learned schedule buys on this workload, with bit-identical distances
+    dist_learned = dist_dev.cpu().numpy().copy()
+    learned_over_reactive = None
+    if plan is not None and sched == _capi.GP_SCHED_LEARNED and not args.only_batched:
+        ropts = _capi.make_opts(_capi.GP_F32, schedule=_capi.GP_SCHED_REACTIVE, grid_kernel=opts.grid_kernel,
+                                queue_tile=opts.queue_tile, local_window=opts.local_window)
+        rplan = _capi.Plan(ctx, [dmesh[mi] for mi, _ in fields],
+                           [(src_dev.data_ptr() + 4 * k, 1) for k in range(F)],
+                           [dist_dev.data_ptr() + 4 * int(voff[k]) for k in range(F)], opts=ropts)
+
+        def reactive():
+            rplan.launch()
+            return None
+
+        ms_reactive, _ = timed(reactive, args.steps, args.warmup, "reactive")
+        rplan.wait()
+        learned_over_reactive = {"ratio": ms_reactive / ms_batched, "ms_reactive": ms_reactive,
+                                 "ms_learned": ms_batched,
+                                 "bit_identical": bool(np.array_equal(dist_dev.cpu().numpy(), dist_learned))}
+        del rplan
+
     # accuracy of the batched result vs the FP64 path of the same library on
     # every field, on the same float-rounded coordinates (the FP64 path is
     # bit-exact with the CPU oracle in the tests)
@@ -328,7 +351,7 @@ def run_gpu(args, rank, world, local):
         "plain_launches": sum(p.launches for p in pstats[-1]), "plain_steps": plain_steps,
         "grid_kernel": {0: "none", 1: "lockstep", 2: "queue"}.get(int(s0.grid_kernel), "?"),
         "tuned": tuned, "graph": plan is not None, "launches_per_step": int(s0.launches),
-        "strong": strong,
+        "strong": strong, "learned_over_reactive": learned_over_reactive,
     }
 
 
@@ -424,12 +447,14 @@ class CpuPtp:
         return self.cache[mi]
 
     def solve(self, mi, src):
+        """One field; src is a vertex or a list of vertices."""
         import oracle
         m = self.mesh(mi)
+        srcs = [int(x) for x in src] if hasattr(src, "__len__") else [int(src)]
         if self.L:
-            return m.geodesics_ptp_cpu([src])
-        _, srt, lim = oracle.toplesets(m, [src])
-        return oracle.ptp(m, [src], lim, srt, nthreads=self.threads)["dist_cpu"]
+            return m.geodesics_ptp_cpu(srcs)
+        _, srt, lim = oracle.toplesets(m, srcs)
+        return oracle.ptp(m, srcs, lim, srt, nthreads=self.threads)["dist_cpu"]
 
 
 def reference_order(n_fields: int, seed: int):
@@ -651,23 +676,60 @@ def main():
                       ("ms_toplesets", "ms_renumber", "ms_local", "ms_grid", "ms_gather")},
         "cpu_baseline": cpu,
         "strong_scaling": res["strong"],
+        "learned_over_reactive": res["learned_over_reactive"],
         "clocks": res["clocks"],
         "gpu_launches": launches,
     }
     emit(out)
 
 
+def sweep_roofline(cs, peak, pkind):
+    """Roofline of a call's dominant sweep launch from its call statistics:
+    48 algorithmic bytes per relaxation over the launch's CUDA-event time."""
+    if cs["ms_grid"] >= cs["ms_local"]:
+        name, ms, relax = "ptp_kernel (grid-wide sweeps)", cs["ms_grid"], cs["relax_grid"]
+    else:
+        name, ms, relax = "ptp_local_kernel (one CTA per field)", cs["ms_local"], cs["relax_local"]
+    ach = ALGO_BYTES_PER_RELAX * relax / (ms * 1e-3) / 1e9 if ms > 0 else 0.0
+    return {"bound": "hbm", "kernel": name, "achieved": ach, "peak": peak, "peak_kind": pkind, "unit": "GB/s",
+            "frac": ach / peak, "traffic": None, "bytes_per_relaxation": ALGO_BYTES_PER_RELAX,
+            "relaxations_per_launch": relax, "ms_per_launch": ms}
+
+
+def cpu_fields(xyz, tri, fields, relax_of=None, budget_fields=None):
+    """The reference's CPU PTP (geodesics PTP_CPU: toplesets + coalescence CPU
+    PTP, FP64, every host core) timed on fields of one mesh.  With relax_of
+    (GPU-counted relaxations per field, same schedule) and budget_fields, only
+    the first budget_fields fields are timed and the rest are scaled by
+    relaxations.  Returns (seconds for all fields, timed fields, kind, cores,
+    estimate?)."""
+    cpu = CpuPtp([("mesh", xyz, tri)])
+    cpu.mesh(0)
+    k = len(fields) if budget_fields is None else min(budget_fields, len(fields))
+    t = 0.0
+    for src in fields[:k]:
+        t0 = time.perf_counter()
+        cpu.solve(0, src)
+        t += time.perf_counter() - t0
+    est = k < len(fields)
+    if est:
+        t *= sum(relax_of) / sum(relax_of[:k])
+    return t, k, cpu.kind, cpu.threads, est
+
+
 def run_config(args):
-    """One of the non-headline workloads; returns its JSON record."""
+    """One of the non-headline workloads; returns its JSON record: the GPU
+    number, the dominant sweep launch's roofline, the reference's CPU PTP on the
+    same workload (timed, or where a full run takes minutes a timed part scaled
+    by the GPU-counted relaxations, marked as an estimate), and the GPU result
+    checked against the FP64 oracle on the same float-rounded coordinates."""
+    import oracle
     from gproshan_gb300 import _capi, build, learned, meshgen
 
     build.build()
     ctx = _capi.Context(0)
     learned.install(ctx)
-
-    def relerr(a, ref):
-        fin = np.isfinite(ref) & (ref > 0)
-        return float(np.max(np.abs(a[fin].astype(np.float64) - ref[fin]) / ref[fin])) if fin.any() else 0.0
+    peak, pkind = peaks()
 
     def best_of(fn, reps):
         best = None
@@ -679,61 +741,126 @@ def run_config(args):
                 best = r + (ctx.call_stats().as_dict(),)
         return best
 
+    def oracle_check(xyz, tri, srcs, dists, iters):
+        om = oracle.Mesh(xyz, tri)
+        x32 = np.asarray(xyz, np.float32).astype(np.float64)
+        err, same = 0.0, 0
+        for src, d, it in zip(srcs, dists, iters):
+            ref = oracle.ptp(om, src, xyz=x32, nthreads=os.cpu_count() or 1)
+            err = max(err, oracle.max_rel_err(d, ref["dist"]))
+            same += int(ref["n_iter"] == it)
+        return {"fields": len(srcs), "max_rel_err_vs_oracle": err, "sweeps_equal_oracle": same,
+                "what": "GPU FP32 vs the FP64 oracle on the same float-rounded coordinates"}
+
     rec = {"config": {"workload": args.config}, "data": "synthetic", "n_gpus": 1, "dtype": "f32"}
     if args.config == "single":
         xyz, tri = meshgen.icosphere(6, 0.1, 0)
         m = _capi.DeviceMesh(ctx, xyz, tri)
-        d32, st32, s32, _ = best_of(lambda: _capi.ptp_batch(ctx, [m], [[0]]), args.steps)
+        d32, st32, s32, cs = best_of(lambda: _capi.ptp_batch(ctx, [m], [[0]]), args.steps)
         d64, st64, s64, _ = best_of(lambda: _capi.ptp_batch(ctx, [m], [[0]], dtype=np.float64, precision=1,
                                                                round_coords=True), max(1, args.steps // 2))
+        t_cpu, nk, kind, cores, est = cpu_fields(xyz, tri, [0])
         rec.update({"metric": "ms per field (plain single-field PTP)", "value": s32 * 1e3, "unit": "ms",
                     "higher_is_better": False, "ms_f64": s64 * 1e3, "n_iter": st32[0].n_iter,
-                    "relaxations": st32[0].relaxations, "max_rel_err": relerr(d32[0], d64[0]),
-                    "config": {"workload": "icosphere L6 (40,962 vertices), source 0"}})
+                    "relaxations": st32[0].relaxations,
+                    "oracle_check": oracle_check(xyz, tri, [[0]], [d32[0]], [st32[0].n_iter]),
+                    "roofline": sweep_roofline(cs, peak, pkind),
+                    "cpu_baseline": {"value": t_cpu * 1e3, "unit": "ms", "cores": cores, "kind": kind,
+                                     "sample": "the same field (toplesets + coalescence CPU PTP, FP64)"},
+                    "config": {"workload": "icosphere L6 (40,962 vertices, jitter 0.1 x mean edge, seed 0), "
+                                           "source 0"}})
     elif args.config == "grid2048":
         xyz, tri = meshgen.height_field(2048, 0)
         src = np.random.default_rng(0).choice(len(xyz), 4, replace=False).astype(np.uint32)
         m = _capi.DeviceMesh(ctx, xyz, tri)
         d32, st32, s32, cs = best_of(lambda: _capi.ptp_batch(ctx, [m], [src]), args.steps)
-        d64, st64, _ = _capi.ptp_batch(ctx, [m], [src], dtype=np.float64, precision=1, round_coords=True)
+        # the reference's CPU PTP on the same family at 512^2 (same seed, 4
+        # sources), scaled by the GPU-counted relaxations of both fields: a
+        # full 2048^2 run takes minutes
+        sx, stri = meshgen.height_field(512, 0)
+        ssrc = np.random.default_rng(0).choice(len(sx), 4, replace=False).astype(np.uint32)
+        sm = _capi.DeviceMesh(ctx, sx, stri)
+        _, sst, _ = _capi.ptp_batch(ctx, [sm], [ssrc])
+        cpu = CpuPtp([("mesh", sx, stri)])
+        cpu.mesh(0)
+        t0 = time.perf_counter()
+        cpu.solve(0, ssrc)
+        t_small = time.perf_counter() - t0
+        t_cpu = t_small * st32[0].relaxations / max(sst[0].relaxations, 1)
         rec.update({"metric": "ms per field", "value": s32 * 1e3, "unit": "ms", "higher_is_better": False,
-                    "n_iter": st32[0].n_iter, "n_iter_f64": st64[0].n_iter, "relaxations": st32[0].relaxations,
-                    "relaxations_per_s": st32[0].relaxations / s32, "max_rel_err": relerr(d32[0], d64[0]),
+                    "n_iter": st32[0].n_iter, "relaxations": st32[0].relaxations,
+                    "relaxations_per_s": st32[0].relaxations / s32,
+                    "oracle_check": oracle_check(xyz, tri, [src], [d32[0]], [st32[0].n_iter]),
+                    "roofline": sweep_roofline(cs, peak, pkind),
                     "phases_ms": {k: cs[k] for k in ("ms_toplesets", "ms_renumber", "ms_local", "ms_grid")},
+                    "cpu_baseline": {"value": t_cpu * 1e3, "unit": "ms", "cores": cpu.threads, "kind": cpu.kind,
+                                     "estimate": True,
+                                     "sample": f"the 512^2 field of the same family ({sst[0].relaxations} "
+                                               f"relaxations, {t_small:.2f} s), scaled by relaxations"},
                     "config": {"workload": "height field 2048^2 (4,194,304 vertices), 4 seeded sources"}})
     elif args.config == "torus":
         xyz, tri = meshgen.torus(400, 2500, seed=0)
         m = _capi.DeviceMesh(ctx, xyz, tri)
         s16 = np.random.default_rng(4).choice(len(xyz), 16, replace=False).astype(np.uint32)
         d1, st1, s1, _ = best_of(lambda: _capi.ptp_batch(ctx, [m], [s16]), args.steps)
-        d64, st64, _ = _capi.ptp_batch(ctx, [m], [s16], dtype=np.float64, precision=1, round_coords=True)
         fs = [[int(x)] for x in s16]
-        _, _, sl, csl = best_of(lambda: _capi.ptp_batch(ctx, [m] * 16, fs, schedule=_capi.GP_SCHED_LEARNED),
-                                args.steps)
+        d16, st16, sl, csl = best_of(lambda: _capi.ptp_batch(ctx, [m] * 16, fs, schedule=_capi.GP_SCHED_LEARNED),
+                                     args.steps)
         _, _, sr, csr = best_of(lambda: _capi.ptp_batch(ctx, [m] * 16, fs), args.steps)
         t_plain = 0.0
         for f in fs:
             t_plain += _capi.ptp_batch(ctx, [m], [f])[2]
-        d16, _, _ = _capi.ptp_batch(ctx, [m] * 16, fs, schedule=_capi.GP_SCHED_LEARNED)
-        d16r, _, _ = _capi.ptp_batch(ctx, [m] * 16, fs, dtype=np.float64, precision=1, round_coords=True)
+        relax16 = [int(x.relaxations) for x in st16]
+        t_cpu, nk, kind, cores, est = cpu_fields(xyz, tri, [f[0] for f in fs], relax16, budget_fields=1)
         rec.update({"metric": "distance fields/s (16 single-source fields, learned schedule)", "value": 16 / sl,
                     "unit": "fields/s", "higher_is_better": True, "reactive_fields_per_s": 16 / sr,
+                    "learned_over_reactive": sr / sl,
                     "plain_fields_per_s": 16 / t_plain, "batched_over_plain": t_plain / sl,
-                    "max_rel_err_16_fields": max(relerr(a, b) for a, b in zip(d16, d16r)),
-                    "one_field_16_sources": {"ms": s1 * 1e3, "n_iter": st1[0].n_iter, "n_iter_f64": st64[0].n_iter,
+                    "oracle_check": oracle_check(xyz, tri, fs[:3], d16[:3], [x.n_iter for x in st16[:3]]),
+                    "roofline": sweep_roofline(csl, peak, pkind),
+                    "cpu_baseline": {"value": 16 / t_cpu, "unit": "fields/s", "cores": cores, "kind": kind,
+                                     "estimate": est,
+                                     "sample": f"{nk} of the 16 fields timed, the rest scaled by their "
+                                               f"GPU-counted relaxations"},
+                    "one_field_16_sources": {"ms": s1 * 1e3, "n_iter": st1[0].n_iter,
                                              "relaxations": st1[0].relaxations,
-                                             "max_rel_err": relerr(d1[0], d64[0])},
+                                             "oracle_check": oracle_check(xyz, tri, [s16], [d1[0]],
+                                                                          [st1[0].n_iter])},
                     "config": {"workload": "torus R=1 r=0.3, 400x2500 (1M vertices), anisotropic (edge ratio "
                                            "up to ~20:1), 16 seeded sources"}})
     else:
         xyz, tri = meshgen.bump_field(1414, 0)
         m = _capi.DeviceMesh(ctx, xyz, tri)
+        _capi.fps(m, 8, seeds=(0,))  # warm-up
         t0 = time.perf_counter()
         smp, md, sec = _capi.fps(m, 512, seeds=(0,))
         wall = time.perf_counter() - t0
+        cs = ctx.call_stats().as_dict()
+        # the oracle's FPS (FP64) over the first samples: FP32 picks the same
+        # farthest vertices while the maxima are separated by more than its
+        # rounding
+        om = oracle.Mesh(xyz, tri)
+        k = 8
+        s_ref, _ = oracle.fps(om, k, [0], nthreads=os.cpu_count() or 1)
+        agree = 0
+        while agree < min(k, len(smp)) and smp[agree] == s_ref[agree]:
+            agree += 1
+        # CPU: the reference has no CPU farthest-point sampling on PTP; its CPU
+        # PTP (toplesets + coalescence CPU PTP) is timed on four of the loop's
+        # fields, the sample sets of 64, 128, 256 and 511 samples the GPU chose
+        # (early fields, with one or a few sources, take minutes each on the CPU)
+        t_cpu, nk, kind, cores, _ = cpu_fields(xyz, tri, [list(smp[:q]) for q in (64, 128, 256, 511)])
         rec.update({"metric": "FPS fields/s (512 sequential geodesic fields)", "value": (len(smp) - 1) / wall,
                     "unit": "fields/s", "higher_is_better": True, "device_s": sec, "wall_s": wall,
                     "samples": len(smp), "max_dist": md,
+                    "oracle_check": {"samples_compared": k, "leading_samples_equal": agree,
+                                     "what": "GPU FP32 samples vs the FP64 oracle's farthest-point samples"},
+                    "roofline": sweep_roofline(cs, peak, pkind) | {"note": "last sample's field"},
+                    "cpu_baseline": {"value": nk / t_cpu, "unit": "fields/s", "cores": cores, "kind": kind,
+                                     "estimate": True,
+                                     "sample": "the reference's CPU PTP on the loop's fields of 64, 128, 256 and "
+                                               "511 sources; these are the cheapest fields of the loop (more "
+                                               "sources, fewer rings), so this overstates the CPU's rate"},
                     "config": {"workload": "bump field 1414^2 (1,999,396 vertices), 64 Gaussian bumps, 5% "
                                            "displaced vertices; farthest-point sampling from vertex 0"}})
     return rec
