@@ -475,6 +475,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		fd.ns = fps->n_init;
 		fd.ns_max = reqs[0].ns;
 		fd.max_dist = INFINITY;
+		fd.first = 0xFFFFFFFFu;
 		GP_CUDA(ctx, stage_copy(o_fps, &fd, sizeof(fd)));
 	}
 	else if(!src_dev)

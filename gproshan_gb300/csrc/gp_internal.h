@@ -135,6 +135,8 @@ struct FpsDev {
 	uint32_t err;               // DEV_ERR_* bits seen by any sample
 	double max_dist;            // max |d| of the last sample's field
 	unsigned long long amax;    // max |d| bits of the current field (gather), reset by the append
+	uint32_t first;             // first vertex holding amax (fps_first_kernel), reset by the append
+	uint32_t pad2;
 };
 
 // Mutable per-field state of the persistent launches.

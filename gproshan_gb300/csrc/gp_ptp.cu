@@ -1594,31 +1594,39 @@ __global__ void normalize_batch_kernel(CatArgs c)
 // src/cuda/geodesics_ptp.cu:122-147): the sample loop runs without a host
 // round trip.  Per sample: fps_sources_kernel sets the field's source count
 // from the device counter, the usual BFS / renumbering / sweeps / gather run
-// (the gather also reduces max |d|), and fps_append_kernel appends the first
-// vertex holding that maximum (cublasI?amax's pick, 0-based) and applies the
-// loop's stop rule.  Once stopped, later samples change nothing.
+// (the gather also reduces max |d|), fps_first_kernel finds the first vertex
+// holding that maximum (cublasI?amax's pick, 0-based) and fps_append_kernel
+// appends it and applies the loop's stop rule.  Once stopped, later samples change nothing.
 // ---------------------------------------------------------------------------
 __global__ void fps_sources_kernel(FieldDev *field, const FpsDev *c)
 {
 	if(threadIdx.x == 0) field->ns = c->ns;
 }
 
+// The first vertex whose |d| is the maximum the gather found (grid-wide:
+// every thread checks its vertices, the smallest index wins).
 template <typename T>
-__global__ void __launch_bounds__(1024) fps_append_kernel(const T *x, uint32_t n, FpsDev *c, uint32_t *samples,
-                                                          double radio, FpsErr e)
+__global__ void fps_first_kernel(const T *x, uint32_t n, FpsDev *c)
 {
-	__shared__ uint32_t s_min;
-	if(threadIdx.x == 0) s_min = 0xFFFFFFFFu;
-	__syncthreads();
 	const unsigned long long m = c->amax;
-	for(uint32_t base = 0; base < n; base += blockDim.x)
-	{
-		const uint32_t i = base + threadIdx.x;
-		if(i < n && (unsigned long long) __double_as_longlong(fabs((double) x[i])) == m) atomicMin(&s_min, i);
-		if(__syncthreads_or(s_min != 0xFFFFFFFFu)) break;
-	}
+	uint32_t best = 0xFFFFFFFFu;
+	for(uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+		if((unsigned long long) __double_as_longlong(fabs((double) x[i])) == m)
+		{
+			best = i;
+			break;
+		}
+	best = __reduce_min_sync(0xffffffffu, best);
+	if((threadIdx.x & 31) == 0 && best != 0xFFFFFFFFu) atomicMin(&c->first, best);
+}
+
+__global__ void fps_append_kernel(FpsDev *c, uint32_t *samples, double radio, FpsErr e)
+{
 	if(threadIdx.x != 0) return;
+	const unsigned long long m = c->amax;
+	const uint32_t first = c->first;
 	c->amax = 0;  // for the next sample
+	c->first = 0xFFFFFFFFu;
 	// this sample's device errors (they are cleared before the next sample runs)
 	uint32_t err = e.sync[0].err | e.sync[1].err | e.bar[2] | e.ctl->err | e.state->status;
 	if(e.wbar) err |= e.wbar[2];
@@ -1627,8 +1635,8 @@ __global__ void __launch_bounds__(1024) fps_append_kernel(const T *x, uint32_t n
 		c->err |= err;
 		c->stop = 1;
 	}
-	if(c->stop || s_min == 0xFFFFFFFFu) return;
-	samples[c->ns] = s_min;
+	if(c->stop || first == 0xFFFFFFFFu) return;
+	samples[c->ns] = first;
 	c->ns++;
 	const double md = __longlong_as_double((long long) m);
 	c->max_dist = md;
@@ -1705,8 +1713,10 @@ cudaError_t launch_fps_sources(FieldDev *field, const FpsDev *c, cudaStream_t s)
 cudaError_t launch_fps_append(const void *dist, bool f64, uint32_t n, FpsDev *c, uint32_t *samples, double radio,
                               const FpsErr &e, cudaStream_t s)
 {
-	if(f64) fps_append_kernel<double><<<1, 1024, 0, s>>>((const double *) dist, n, c, samples, radio, e);
-	else fps_append_kernel<float><<<1, 1024, 0, s>>>((const float *) dist, n, c, samples, radio, e);
+	const unsigned nb = grid_for(n);
+	if(f64) fps_first_kernel<double><<<nb, 256, 0, s>>>((const double *) dist, n, c);
+	else fps_first_kernel<float><<<nb, 256, 0, s>>>((const float *) dist, n, c);
+	fps_append_kernel<<<1, 32, 0, s>>>(c, samples, radio, e);
 	return cudaGetLastError();
 }
 
