@@ -576,6 +576,51 @@ def reference_arm(args):
             "e2e": {"value": v, "unit": "fields/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
 
 
+def reference_gpu_arm(args):
+    """`--impl reference_gpu` (not part of the driver's arms): the reference's
+    own GPU PTP -- geodesics(mesh, sources, PTP_GPU), i.e. che::compute_toplesets
+    on the host, then parallel_toplesets_propagation_coalescence_gpu
+    (src/cuda/geodesics_ptp_coalescence.cu, one source) -- built unmodified for
+    sm_103a, over every field of the workload, one call per field as its
+    callers make them.  Each call resets the device, so this mode runs no other
+    GPU code in its process.  Reports wall-clock fields/s and the GPU time the
+    reference's own event timer reports; fields on meshes of at most 50k
+    vertices are checked against the FP64 oracle."""
+    import oracle
+    L = oracle.RefGpuLib(oracle.build_ref_gpu())
+    meshes, fields = make_workload(shard_seed(args.seed, 0), args.meshes)
+    hs = []
+    for _, xyz, tri in meshes:
+        x = np.ascontiguousarray(np.asarray(xyz, np.float32).astype(np.float64).reshape(-1))
+        t = np.ascontiguousarray(np.asarray(tri, np.uint32).reshape(-1))
+        hs.append(L.create(x, len(x) // 3, t, len(t) // 3))
+    small = min(range(len(fields)), key=lambda k: len(meshes[fields[k][0]][1]))
+    for _ in range(max(args.warmup, 1)):
+        mi, s = fields[small]
+        L.geod(hs[mi], np.array([s], np.uint32), 1, np.empty(len(meshes[mi][1])))
+    wall, rep, err, checked = 0.0, 0.0, 0.0, 0
+    for mi, s in fields:
+        d = np.empty(len(meshes[mi][1]))
+        t0 = time.perf_counter()
+        rep += L.geod(hs[mi], np.array([s], np.uint32), 1, d)
+        wall += time.perf_counter() - t0
+        if len(d) <= 50_000:
+            om = oracle.Mesh(np.asarray(meshes[mi][1], np.float32).astype(np.float64), meshes[mi][2])
+            err = max(err, oracle.max_rel_err(d, oracle.ptp(om, [s])["dist"]))
+            checked += 1
+    for h in hs:
+        L.free(h)
+    F = len(fields)
+    return {"impl": "reference_gpu", "metric": METRIC, "value": F / wall, "unit": "fields/s", "n_gpus": 1,
+            "higher_is_better": True, "dtype": "f64", "data": "synthetic",
+            "wall_s": wall, "reference_reported_gpu_s": rep, "reported_fields_per_s": F / rep if rep else None,
+            "oracle_check": {"fields": checked, "max_rel_err_vs_oracle": err},
+            "config": {"workload": WORKLOAD, "fields": F},
+            "what": "the reference's own GPU PTP (geodesics PTP_GPU: host toplesets + "
+                    "parallel_toplesets_propagation_coalescence_gpu, FP64, built for sm_103a), one call per field; "
+                    "wall clock per call, and the time its own event timer reports (device reset to download)"}
+
+
 def emit(obj):
     print(json.dumps(obj), flush=True)
 
@@ -585,7 +630,7 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference", "reference_gpu"])
     ap.add_argument("--seed", type=int, default=2024)
     ap.add_argument("--skip-check", action="store_true")
     ap.add_argument("--meshes", type=int, default=N_MESHES, help="meshes in the workload (profiling runs)")
@@ -614,6 +659,10 @@ def main():
     if args.impl == "reference":
         if rank == 0:
             emit(reference_arm(args))
+        return
+    if args.impl == "reference_gpu":
+        if rank == 0:
+            emit(reference_gpu_arm(args))
         return
 
     res = run_gpu(args, rank, world, local)

@@ -58,6 +58,33 @@ def build(ref: bool | None = None, ref_dir: str | None = None) -> None:
         subprocess.run(["make", "-s", "-C", HERE, "ref", f"REF={src}"], check=True)
 
 
+def build_ref_gpu() -> str:
+    """Compile _ref/libref_gpu_f64.so: the reference's own GPU PTP (sm_103a)
+    with its CPU che, from the reference sources (see reference_sources()).
+    Returns its path.  It resets the device on every call: load it only in a
+    process that uses no other GPU code."""
+    src = reference_sources()
+    if src is None:
+        raise FileNotFoundError("reference sources not present (GPROSHAN_REF or the staged copy)")
+    subprocess.run(["make", "-s", "-C", HERE, "ref_gpu", f"REF={src}"], check=True)
+    return os.path.join(HERE, "_ref", "libref_gpu_f64.so")
+
+
+class RefGpuLib:
+    """ctypes view of _ref/libref_gpu_f64.so (ref_wrap.cpp built with REF_GPU)."""
+
+    def __init__(self, path: str):
+        L = C.CDLL(path)
+        self.create = L.refg_f64_che_create
+        self.create.restype = C.c_void_p
+        self.create.argtypes = [_f64p, C.c_uint, _u32p, C.c_uint]
+        self.free = L.refg_f64_che_free
+        self.free.argtypes = [C.c_void_p]
+        self.geod = L.refg_f64_geodesics_ptp_gpu
+        self.geod.restype = C.c_double
+        self.geod.argtypes = [C.c_void_p, _u32p, C.c_uint, _f64p]
+
+
 class _OrcInfo(C.Structure):
     _fields_ = [("n_iter", C.c_uint32), ("last", C.c_uint32), ("relaxations", C.c_uint64)]
 

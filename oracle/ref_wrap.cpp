@@ -20,7 +20,11 @@
  *
  * Built twice: once with real_t = double (the reference default) and once
  * with -DSINGLE_P (real_t = float).  The C entry points carry a suffix so
- * both libraries can be loaded into one process.
+ * both libraries can be loaded into one process.  A third build (-DREF_GPU,
+ * prefix refg_f64_) also links the reference's own GPU PTP
+ * (src/cuda/geodesics_ptp.cu, geodesics_ptp_coalescence.cu, che.cu,
+ * vertex.cu) and exposes geodesics_ptp_gpu; that path calls cudaDeviceReset on
+ * every call, so it is only ever loaded by a process of its own.
  */
 #include "che.h"
 #include "che_off.h"
@@ -30,7 +34,9 @@
 #include <cstring>
 #include <vector>
 
-#ifdef SINGLE_P
+#if defined(REF_GPU)
+#define REFW(name) refg_f64_##name
+#elif defined(SINGLE_P)
 #define REFW(name) refw_f32_##name
 #else
 #define REFW(name) refw_f64_##name
@@ -166,6 +172,32 @@ unsigned REFW(geodesics_ptp_cpu)(void * h, const unsigned * src, unsigned n_src,
 	gproshan::parallel_toplesets_propagation_coalescence_cpu({dist, nullptr}, m, sources, {limits, s});
 	return (unsigned) limits.size();
 }
+
+#ifdef REF_GPU
+/*
+ * One field the way geodesics(mesh, sources, PTP_GPU) computes it
+ * (src/geodesics.cpp:16-33 and run_parallel_toplesets_propagation_gpu,
+ * :225-240): dist set to INFINITY, che::compute_toplesets on the host, then
+ * parallel_toplesets_propagation_coalescence_gpu for one source or
+ * parallel_toplesets_propagation_gpu for several.  Returns the GPU seconds the
+ * reference itself reports.
+ */
+double REFW(geodesics_ptp_gpu)(void * h, const unsigned * src, unsigned n_src, distance_t * dist)
+{
+	che * m = (che *) h;
+	const size_t n = m->n_vertices();
+	for(size_t v = 0; v < n; v++)
+		dist[v] = INFINITY;
+	std::vector<index_t> sources(src, src + n_src);
+	std::vector<index_t> toplesets(n), sorted(n + n_src), limits;
+	index_t * r = toplesets.data();
+	index_t * s = sorted.data();
+	m->compute_toplesets(r, s, limits, sources);
+	if(sources.size() > 1)
+		return gproshan::parallel_toplesets_propagation_gpu({dist, nullptr}, m, sources, {limits, s});
+	return gproshan::parallel_toplesets_propagation_coalescence_gpu({dist, nullptr}, m, sources, {limits, s});
+}
+#endif
 
 distance_t REFW(update_step)(void * h, const distance_t * dist, unsigned he)
 {
