@@ -300,6 +300,12 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		fbase[f] = (uint32_t) ftot;
 		sbase[f] = (uint32_t) stot;
 		const uint64_t S = (uint64_t) nv + r.ns + 2;
+		if(stage == Stage::ptp && !f64 && S >= FIELD_MAX_SLOTS_F32)
+		{
+			set_err(ctx, "field %u: %llu vertices and sources exceed the FP32 path's 2^27 per field (use GP_F64)", f,
+			        (unsigned long long) S);
+			return GP_ERR_CAPACITY;
+		}
 		tot += S;
 		vtot += nv;
 		ftot += (uint64_t) r.mesh->dev.n_fan + (uint64_t) r.ns * r.mesh->dev.max_fan;

@@ -21,6 +21,12 @@ constexpr uint32_t MAX_WALK = 1u << 16;       // longest star walk accepted per 
 // CSR lists (off/fan) instead.
 constexpr uint32_t FAN8_EMPTY = 0xFFFFFFFFu;
 constexpr uint32_t FAN8_OVERFLOW = 0xFFFFFFFEu;
+// Slot 0 of a renumbered field row (the FP32 sweeps' rows) also carries the
+// row's entry count: bit 31 closed, bits 27-30 count (0-8), bits 0-26 the
+// first neighbour (a field's renumbered ids stay below 2^27, checked on the host).
+constexpr uint32_t FAN8_N_SHIFT = 27;
+constexpr uint32_t FAN8_ID_MASK = (1u << FAN8_N_SHIFT) - 1u;
+constexpr uint64_t FIELD_MAX_SLOTS_F32 = 1ull << FAN8_N_SHIFT;
 
 // trig/next/prev of the compact half-edge mesh (src/che.cpp:18-34)
 __host__ __device__ inline uint32_t he_next(uint32_t he) { return 3 * (he / 3) + (he + 1) % 3; }

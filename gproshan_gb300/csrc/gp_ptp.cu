@@ -445,12 +445,10 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 	vd = unflag(vs);
 	const float4 pv = __ldg(F.P + v);
 	if(CL) lab = ld_d<uint32_t, COH>(Co + v);
-	uint32_t u[FB] = {ra.x & FAN_MASK, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
-	const bool closed = (ra.x & FAN_CLOSED) != 0 && ra.x != FAN8_EMPTY;
+	uint32_t u[FB] = {ra.x & FAN8_ID_MASK, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+	const bool closed = (ra.x & FAN_CLOSED) != 0;
 	if(rb.w == FAN8_OVERFLOW) return relax32_csr<CL, COH>(F, v, Do, Co, lab, vd, pv);
-	uint32_t n = 0;
-#pragma unroll
-	for(uint32_t k = 0; k < FB; k++) n += (k == 0 ? ra.x : u[k]) != FAN8_EMPTY;
+	const uint32_t n = (ra.x >> FAN8_N_SHIFT) & 15u;
 	if(!n) return vd;
 	// inputs unchanged since the previous sweep: the value stands (labels
 	// always take the full path: a tie can move a label without a distance)
@@ -1472,8 +1470,11 @@ __global__ void fill_kernel(CatArgs c)
 				if(n > 8) r[7] = FAN8_OVERFLOW;
 				// the star keeps the reference's triangle order (che::link from
 				// EVT), so the label rule's "first strictly smaller candidate"
-				// picks the same triangle as the reference in exact ties
-				if(n && (o0f & FAN_CLOSED)) r[0] |= FAN_CLOSED;
+				// picks the same triangle as the reference in exact ties.  Slot 0
+				// packs closed | count | first neighbour (see FAN8_N_SHIFT)
+				r[0] = n ? (r[0] & FAN8_ID_MASK) | ((n <= 8 ? n : 0u) << FAN8_N_SHIFT) |
+				               ((o0f & FAN_CLOSED) ? FAN_CLOSED : 0u)
+				         : 0u;
 				F.fan8[2 * (size_t) k] = make_uint4(r[0], r[1], r[2], r[3]);
 				F.fan8[2 * (size_t) k + 1] = make_uint4(r[4], r[5], r[6], r[7]);
 			}
@@ -1505,7 +1506,7 @@ __global__ void fill_kernel(CatArgs c)
 		else if(k == nr)
 		{
 			F.off[k] = c.cnt[g];
-			F.fan8[2 * (size_t) k] = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);
+			F.fan8[2 * (size_t) k] = make_uint4(0u, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);  // count 0
 			F.fan8[2 * (size_t) k + 1] = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);
 			F.P[k] = make_float4(0.f, 0.f, 0.f, 0.f);
 			if(F.Pd)
