@@ -13,7 +13,13 @@
 //   * errors are reported (gproshan_error + INFINITY distances) instead of
 //     being ignored;
 //   * distance_t may be double (default build) or float (SINGLE_P): the
-//     library writes either type directly.
+//     library writes either type directly.  A double build computes in FP64
+//     by default (the reference formula, bit-exact with the reference's
+//     arithmetic); the environment variable GP_PTP_PRECISION=f32 makes it
+//     compute in FP32 instead (within 1e-5 of FP64; about 50x faster on
+//     GB300, whose FP64 pipe is narrow), still writing doubles.
+#include <cstdlib>
+#include <cstring>
 #include "geodesics_ptp.h"
 
 #include "gp_ptp.h"
@@ -45,6 +51,19 @@ gp_ctx *thread_ctx()
 
 constexpr gp_dtype dist_type = sizeof(distance_t) == sizeof(double) ? GP_F64 : GP_F32;
 
+// Arithmetic of the solve: distance_t's, unless GP_PTP_PRECISION says
+// otherwise ("f32" or "f64"); read once per process.
+uint32_t precision()
+{
+	static const uint32_t p = [] {
+		const char *e = std::getenv("GP_PTP_PRECISION");
+		if(e && !std::strcmp(e, "f32")) return (uint32_t) GP_F32;
+		if(e && !std::strcmp(e, "f64")) return (uint32_t) GP_F64;
+		return (uint32_t) dist_type;
+	}();
+	return p;
+}
+
 // Upload the che (GT/VT/OT/EVT, as cuda_create_CHE does, src/cuda/che.cu:29-48).
 gp_mesh *upload(gp_ctx *ctx, che *mesh)
 {
@@ -72,7 +91,7 @@ double run(const ptp_out_t &ptp_out, che *mesh, const std::vector<index_t> &sour
 	gp_mesh *m = ctx ? upload(ctx, mesh) : nullptr;
 	gp_ptp_stats stats{};
 	gp_ptp_opts opts{};
-	opts.precision = dist_type;  // FP64 builds run the reference formula in FP64
+	opts.precision = precision();  // FP64 builds run the reference formula in FP64 unless told otherwise
 	gp_status st = GP_ERR_NO_DEVICE;
 	if(m)
 		st = gp_ptp(ctx, m, sources.data(), (uint32_t) sources.size(), toplesets.limits.data(),
@@ -132,7 +151,7 @@ distance_t farthest_point_sampling_ptp_gpu(che *mesh, std::vector<index_t> &samp
 	uint32_t n_out = 0;
 	double md = INFINITY, sec = 0;
 	gp_ptp_opts opts{};
-	opts.precision = dist_type;
+	opts.precision = precision();
 	const gp_status st = m ? gp_fps(ctx, m, s.data(), (uint32_t) samples.size(), (uint32_t) cap, n, radio, &opts,
 	                                &n_out, &md, &sec)
 	                       : GP_ERR_NO_DEVICE;

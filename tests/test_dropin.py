@@ -49,13 +49,13 @@ def dropin_exe(tmp_path_factory, built_lib):
     return out
 
 
-def _run(exe, d, xyz, tri, src, n_fps):
+def _run(exe, d, xyz, tri, src, n_fps, env=None):
     os.makedirs(d, exist_ok=True)
     np.ascontiguousarray(xyz, np.float64).tofile(os.path.join(d, "xyz.f64"))
     np.ascontiguousarray(tri, np.uint32).tofile(os.path.join(d, "tri.u32"))
     np.asarray(src, np.uint32).tofile(os.path.join(d, "src.u32"))
     np.asarray([n_fps], np.uint32).tofile(os.path.join(d, "fps.u32"))
-    r = subprocess.run([exe, d], capture_output=True, text=True, timeout=600)
+    r = subprocess.run([exe, d], capture_output=True, text=True, timeout=600, env=env)
     assert r.returncode == 0, (r.returncode, r.stderr[-2000:])
     rd = lambda n, t: np.fromfile(os.path.join(d, n), dtype=t)
     return {k: rd(k, np.float64) for k in ("gpu.dist", "gpu_reset.dist", "coal.dist")} | \
@@ -97,3 +97,21 @@ def test_dropin_coalescence_keeps_caller_values_on_unreached_vertices(dropin_exe
     assert (out["coal.dist"][~first] == -7).all() and (out["coal.cl"][~first] == 12345).all()
     assert np.array_equal(out["coal.cl"][first], ref["clusters"][first])
     assert np.array_equal(out["gpu_reset.dist"], out["gpu.dist"])
+
+
+def test_dropin_fp32_opt_in(dropin_exe, oracle_lib, tmp_path):
+    """GP_PTP_PRECISION=f32: a double build computes in FP32 and still writes
+    doubles: within 1e-5 of the FP64 oracle on the float-rounded coordinates
+    the FP32 path reads, labels and FPS samples equal to the oracle's."""
+    from gproshan_gb300 import meshgen
+    xyz, tri = meshgen.icosphere(4, 0.1, 3)
+    src = [0, 1500, 2000]
+    env = dict(os.environ, GP_PTP_PRECISION="f32")
+    out = _run(dropin_exe, str(tmp_path / "f32"), xyz, tri, src, 9, env=env)
+    om = oracle_lib.Mesh(xyz, tri)
+    x32 = xyz.astype(np.float32).astype(np.float64)
+    ref = oracle_lib.ptp(om, src, clusters=True, xyz=x32)
+    assert oracle_lib.max_rel_err(out["gpu.dist"], ref["dist"]) <= 1e-5
+    assert not np.array_equal(out["gpu.dist"], oracle_lib.ptp(om, src)["dist"])  # not the FP64 path
+    assert np.array_equal(out["gpu.cl"], ref["clusters"])
+    assert np.array_equal(out["fps_samples.u32"], oracle_lib.fps(om, 9, [0])[0])

@@ -104,3 +104,23 @@ def test_autotune_choice_keeps_results(gpu_ctx):
                                            _capi.C.byref(sec)), "gp_ptp_batch")
     for k in range(len(ms)):
         assert np.array_equal(outs[k], ref[k]), k
+
+
+def test_sharded_front_end_on_one_rank(gpu_ctx):
+    """gproshan_gb300.shard on a single process: the cost model's predicted
+    relaxations come from the GPU (toplesets features + BF16 MLP), are positive
+    and grow with the mesh, and ptp_sharded returns every field, in the
+    caller's order, bit for bit equal to one gp_ptp_batch call."""
+    from gproshan_gb300 import _capi, meshgen, shard
+    ms = [_capi.DeviceMesh(gpu_ctx, *meshgen.icosphere(3, 0.1, 1)),
+          _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(120, 2)),
+          _capi.DeviceMesh(gpu_ctx, *meshgen.icosphere(5, 0.1, 3))]
+    meshes = [ms[0], ms[1], ms[2], ms[1], ms[0]]
+    srcs = [[0], [5], [17], [9000, 3], [600]]
+    c = shard.predicted_costs(gpu_ctx, meshes, srcs)
+    assert c.shape == (5,) and np.all(c > 0) and c[2] > c[0]
+    full, mine, parts = shard.ptp_sharded(gpu_ctx, meshes, srcs)
+    assert parts == [list(range(5))] and mine == list(range(5))
+    ref, _, _ = _capi.ptp_batch(gpu_ctx, meshes, srcs)
+    for a, b in zip(full, ref):
+        assert np.array_equal(a, b)
