@@ -183,12 +183,14 @@ __device__ __forceinline__ double update64(const Nb64 &A0, const Nb64 &A1)
 	const double t0 = A0.t, t1 = A1.t;
 	const double q00 = dot64(X0x, X0y, X0z, X0x, X0y, X0z);
 	const double q01 = dot64(X0x, X0y, X0z, X1x, X1y, X1z);
-	const double q10 = dot64(X1x, X1y, X1z, X0x, X0y, X0z);
+	// q10 = X1.X0 equals q01 bit for bit (IEEE products commute and the sums
+	// run in the same order), hence Q10 == Q01: one division fewer
+	const double q10 = q01;
 	const double q11 = dot64(X1x, X1y, X1z, X1x, X1y, X1z);
 	const double det = __dsub_rn(__dmul_rn(q00, q11), __dmul_rn(q01, q10));
 	const double Q00 = __ddiv_rn(q11, det);
 	const double Q01 = __ddiv_rn(-q01, det);
-	const double Q10 = __ddiv_rn(-q10, det);
+	const double Q10 = Q01;
 	const double Q11 = __ddiv_rn(q00, det);
 	const double delta = __dadd_rn(__dmul_rn(t0, __dadd_rn(Q00, Q10)), __dmul_rn(t1, __dadd_rn(Q01, Q11)));
 	const double sQ = __dadd_rn(__dadd_rn(__dadd_rn(Q00, Q01), Q10), Q11);
