@@ -692,15 +692,24 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		fps->max_dist = hfps.max_dist;
 	}
 	if(stage == Stage::ptp && !out_dev && !fps)
-		for(uint32_t f = 0; f < F; f++)
+	{
+		// the fields' outputs lie back to back in the workspace; runs of fields
+		// whose host arrays also lie back to back go down in one copy
+		for(uint32_t f0 = 0; f0 < F;)
 		{
-			const size_t nv = reqs[f].mesh->nv;
-			GP_CUDA(ctx, cudaMemcpyAsync(reqs[f].dist, P(o_out) + (size_t) vbase[f] * osz, nv * osz,
-			                             cudaMemcpyDeviceToHost, s));
+			uint32_t f1 = f0 + 1;
+			while(f1 < F && static_cast<char *>(reqs[f1].dist) ==
+			                    static_cast<char *>(reqs[f1 - 1].dist) + (size_t) reqs[f1 - 1].mesh->nv * osz)
+				f1++;
+			GP_CUDA(ctx, cudaMemcpyAsync(reqs[f0].dist, P(o_out) + (size_t) vbase[f0] * osz,
+			                             (size_t) (vbase[f1] - vbase[f0]) * osz, cudaMemcpyDeviceToHost, s));
+			f0 = f1;
+		}
+		for(uint32_t f = 0; f < F; f++)
 			if(reqs[f].clusters)
 				GP_CUDA(ctx, cudaMemcpyAsync(reqs[f].clusters, reinterpret_cast<uint32_t *>(P(o_cout)) + vbase[f],
-				                             4 * nv, cudaMemcpyDeviceToHost, s));
-		}
+				                             4 * (size_t) reqs[f].mesh->nv, cudaMemcpyDeviceToHost, s));
+	}
 	GP_CUDA(ctx, cudaStreamSynchronize(s));
 	uint32_t ferr = 0;
 	for(uint32_t f = 0; f < F; f++) ferr |= hs[f].status;

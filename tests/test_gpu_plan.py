@@ -124,3 +124,29 @@ def test_sharded_front_end_on_one_rank(gpu_ctx):
     ref, _, _ = _capi.ptp_batch(gpu_ctx, meshes, srcs)
     for a, b in zip(full, ref):
         assert np.array_equal(a, b)
+
+
+def test_host_outputs_back_to_back_and_scattered(gpu_ctx):
+    """Host output arrays that lie back to back in one buffer (downloaded in
+    merged copies) and arrays scattered in memory give the same distances."""
+    import ctypes as C
+    from gproshan_gb300 import _capi, meshgen
+    ms = [_capi.DeviceMesh(gpu_ctx, *meshgen.icosphere(3, 0.1, 1)),
+          _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(90, 2))]
+    meshes = [ms[0], ms[1], ms[1], ms[0], ms[1]]
+    srcs = [[0], [5], [70], [9], [8000]]
+    ref, _, _ = _capi.ptp_batch(gpu_ctx, meshes, srcs)
+    nv = [m.n_vertices for m in meshes]
+    buf = np.full(sum(nv) + 7, -1.0, np.float32)
+    off = np.concatenate([[0], np.cumsum(nv)])
+    # fields 0-2 back to back, field 3 after a gap, field 4 in its own array
+    views = [buf[off[0]:off[1]], buf[off[1]:off[2]], buf[off[2]:off[3]], buf[off[3] + 7:off[4] + 7],
+             np.empty(nv[4], np.float32)]
+    fields, keep = _capi._fields(meshes, srcs, views)
+    o = _capi.make_opts(_capi.GP_F32)
+    sec = C.c_double()
+    gpu_ctx.check(_capi.lib().gp_ptp_batch(gpu_ctx.handle, fields, len(meshes), C.byref(o), _capi.GP_F32, 0,
+                                           C.byref(sec)), "gp_ptp_batch")
+    for a, b in zip(views, ref):
+        assert np.array_equal(a, b)
+    assert (buf[off[3]:off[3] + 7] == -1.0).all()  # the gap is left alone
