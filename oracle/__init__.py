@@ -45,12 +45,16 @@ def reference_sources() -> str | None:
 def build(ref: bool | None = None, ref_dir: str | None = None) -> None:
     """Compile the oracle and, when the reference's sources are at hand
     (``ref_dir``, GPROSHAN_REF or the staged copy), the reference's own CPU
-    code into _ref/.  With GPROSHAN_REF set, its sources are first staged
+    code into _ref/.  With GPROSHAN_REF set -- or, without a staged copy, with
+    the Makefile's default checkout present -- its sources are first staged
     into baseline/_ref/ so that they travel with the working tree."""
     subprocess.run(["make", "-s", "-C", HERE, "liboracle.so"], check=True)
     env = os.environ.get("GPROSHAN_REF")
     if env and os.path.isfile(os.path.join(env, "src", "geodesics_ptp.cpp")):
         subprocess.run(["make", "-s", "-C", HERE, "stage", f"GPROSHAN_REF={env}"], check=True)
+    elif not os.path.isfile(os.path.join(STAGED_REF, "src", "geodesics_ptp.cpp")):
+        # no staged copy: stage from the recipe's default checkout if there is one
+        subprocess.run(["make", "-s", "-C", HERE, "stage"], capture_output=True)
     src = ref_dir or reference_sources()
     if ref is None:
         ref = src is not None
