@@ -638,3 +638,34 @@ def test_high_valence_poles_on_the_grid_launch(gpu_ctx, oracle_lib, src):
     assert oracle_lib.max_rel_err(d32, ref32["dist"]) <= REL_TOL_F32
     d32c, _, _ = _capi.ptp(m, src, clusters=np.zeros(len(xyz), np.uint32), opts=_capi.make_opts(_capi.GP_F32, **kw))
     assert np.array_equal(d32, d32c)
+
+
+@pytest.mark.parametrize("n,seeds,radio", [(10000, [0, 50], 0.0), (20, [3], 10.0), (1, [3], 0.0), (30, [7, 7], 0.0)],
+                         ids=["n_above_vertices", "radius_at_first", "no_new_sample", "repeated_seed"])
+def test_fps_device_loop_edge_cases(gpu_ctx, oracle_lib, n, seeds, radio):
+    """The device sample loop at its edges, against the oracle (FP64 path):
+    n at or above the vertex count is clamped to half of it, as the reference
+    does; a radius larger than the first field's farthest distance stops after
+    one new sample; n not above the seeds adds nothing; a repeated seed."""
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.icosphere(2, 0.1, 5)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    om = oracle_lib.Mesh(xyz, tri)
+    s_ref, md_ref = oracle_lib.fps(om, n, seeds, radio=radio)
+    s, md, _ = _capi.fps(m, n, seeds, radio=radio, precision=_capi.GP_F64)
+    assert np.array_equal(s, s_ref)
+    assert md == md_ref or (np.isinf(md) and np.isinf(md_ref))
+
+
+def test_normalize_option_with_labels(gpu_ctx, oracle_lib):
+    """normalize and cluster labels in one FP64 call: distances are
+    normalize_ptp of the plain ones, labels unchanged, bit for bit."""
+    from gproshan_gb300 import _capi, meshgen
+    xyz, tri = meshgen.icosphere(4, 0.1, 2)
+    m = dev_mesh(gpu_ctx, xyz, tri)
+    src = [0, 1000, 2000]
+    d0, c0, _ = _capi.ptp(m, src, dtype=np.float64, precision=_capi.GP_F64, clusters=np.zeros(len(xyz), np.uint32))
+    d1, c1, _ = _capi.ptp(m, src, dtype=np.float64, clusters=np.zeros(len(xyz), np.uint32),
+                          opts=_capi.make_opts(_capi.GP_F64, normalize=True))
+    assert np.array_equal(c0, c1)
+    assert np.array_equal(d1, oracle_lib.normalize_ptp(d0))
