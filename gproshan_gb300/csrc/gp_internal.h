@@ -15,10 +15,12 @@ constexpr uint32_t NIL = 0xFFFFFFFFu;
 constexpr uint32_t FAN_CLOSED = 0x80000000u;  // bit 31 of fan_off[v]: v's fan is closed
 constexpr uint32_t FAN_MASK = 0x7FFFFFFFu;
 constexpr uint32_t MAX_WALK = 1u << 16;       // longest star walk accepted per vertex
-// Fixed-stride fan rows of the renumbered copy: slots 0..n-1 hold the fan,
-// unused slots FAN8_EMPTY; bit 31 of slot 0 marks a closed fan; a vertex with
-// more than 8 fan entries has slot 7 = FAN8_OVERFLOW and is read from the
-// CSR lists (off/fan) instead.
+// Fixed-stride fan rows: slots 0..n-1 hold the fan; bit 31 of slot 0 marks a
+// closed fan; a vertex with more than 8 fan entries has slot 7 = FAN8_OVERFLOW
+// and is read from the CSR lists (off/fan) instead.  The mesh's own rows mark
+// unused slots FAN8_EMPTY.  The renumbered rows of a field pad them instead: a
+// closed fan repeats its first neighbour in slot n, the remaining slots repeat
+// the last entry written, and a closed fan of 8 entries overflows.
 constexpr uint32_t FAN8_EMPTY = 0xFFFFFFFFu;
 constexpr uint32_t FAN8_OVERFLOW = 0xFFFFFFFEu;
 // Slot 0 of a renumbered field row (the FP32 sweeps' rows) also carries the

@@ -377,6 +377,20 @@ __device__ __forceinline__ Nb32 make_nb(float4 pu, float2 t, float4 pv, uint32_t
 	return n;
 }
 
+__device__ __forceinline__ Nb32 make_nb_lean(float4 pu, float2 t, float4 pv)
+{
+	Nb32 n;
+	n.x = pu.x - pv.x;
+	n.y = pu.y - pv.y;
+	n.z = pu.z - pv.z;
+	n.t = t.x;
+	n.te = t.y;
+	n.q = fmaf(n.x, n.x, fmaf(n.y, n.y, n.z * n.z));
+	n.l = sqrt_a(n.q);
+	n.u = 0;
+	return n;
+}
+
 // Relaxation of one vertex on the FP32 path: new = min(old, star updates),
 // with the strict `if(p < best)` order of the reference (relax_ptp,
 // src/cuda/geodesics_ptp.cu:234-282).  All fan indices of a vertex of valence
@@ -384,6 +398,11 @@ __device__ __forceinline__ Nb32 make_nb(float4 pu, float2 t, float4 pv, uint32_t
 // registers, several loads in flight).  Returns the new (hi, lo) pair.
 #ifndef GP_FC
 #define GP_FC 2
+#endif
+// Unlabelled FP32 sweeps take relax32_lean (1) or the triangle-by-triangle
+// relax32 (0, a measurement build).
+#ifndef GP_LEAN
+#define GP_LEAN 1
 #endif
 constexpr uint32_t FC = GP_FC;
 
@@ -512,6 +531,170 @@ __device__ __forceinline__ float2 relax32(const FieldDev &F, uint32_t v, const f
 	return df_result(bh, bl, best);
 }
 
+// ---------------------------------------------------------------------------
+// Lean FP32 relaxation (distances only, no labels).
+//
+// The reference takes, per star triangle, either the planar solution or the
+// edge fallback min(t0 + |X0|, t1 + |X1|), then the minimum over the star.
+// Where the planar test passes, the planar value is the distance from a
+// virtual source S with |S - x0| = t0 and |S - x1| = t1, so by the triangle
+// inequality it is <= t0 + |X0| and <= t1 + |X1|.  Hence the minimum over the
+// star equals the minimum of (a) every neighbour's edge value t_k + |X_k| and
+// (b) the planar values of the triangles whose test passes -- provided every
+// neighbour lies on a triangle (two or more fan entries) and no triangle is
+// degenerate (the reference ignores a degenerate triangle with finite inputs,
+// edge values included).  Each edge value is then formed once per neighbour
+// instead of twice per triangle, and a triangle carries no fallback selection.
+// A vertex whose star has a degenerate triangle (A^2 not > 0) is relaxed again
+// by the triangle-by-triangle path (relax32), so the reference's rule holds
+// exactly there.  The two formulations agree to rounding: the only difference
+// is which of two candidates equal to within an ulp of an edge is kept.
+//
+// The padded rows (FAN8_*) make every slot a real neighbour and every star
+// triangle a pair of consecutive slots (the closing one too), so the lanes of
+// a warp walk the same number of slots -- the warp's longest row -- with no
+// per-slot branch: a slot past a lane's own row repeats its last entry, whose
+// edge value is already a candidate and whose pair of equal ids is no
+// triangle (its planar test compares NaN; it is exempt from the degenerate
+// check).
+//
+// INF neighbours need no test: their relative offset comes out NaN, every
+// comparison with it is false, and a NaN offset never passes the planar test
+// (max(r, 0) is then 0 and the tests compare NaN), which is the reference's
+// "INF inputs take the edge fallback" -- the other neighbour's edge value is
+// a candidate of its own.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float2 rel_to_lean(float2 dv, float bh, float bl)
+{
+	float h, eh;
+	two_sum(dv.x, -bh, h, eh);
+	const float l = (dv.y - bl) + eh;
+	const float t = h + l;
+	return make_float2(t, l - (t - h));
+}
+
+// The running best (value, and the operands its exact value is formed from).
+struct Best32 {
+	float p, t, x, te;
+};
+
+__device__ __forceinline__ void take_edge(const Nb32 &k, Best32 &b)
+{
+	const float d = k.t + k.l;
+	if(d < b.p) b = {d, k.t, k.l, k.te};
+}
+
+// Planar candidate of triangle (a, b).  A degenerate triangle (A^2 not > 0)
+// of two distinct vertices sets best.p to -INF, which no later candidate
+// beats and which sends the vertex to the triangle-by-triangle path.
+__device__ __forceinline__ void take_planar(const Nb32 &a, const Nb32 &b, bool distinct, Best32 &best)
+{
+	const float ex = b.x - a.x, ey = b.y - a.y, ez = b.z - a.z;
+	const float e2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+	const float a1 = -fmaf(a.x, ex, fmaf(a.y, ey, a.z * ez));  // -X0.E
+	const float a0 = e2 - a1;                                 // X1.E = E.E + X0.E
+	const float q01 = a.q - a1;                               // X0.X1 = X0.X0 + X0.E
+	const float cx = fmaf(a.y, b.z, -a.z * b.y);
+	const float cy = fmaf(a.z, b.x, -a.x * b.z);
+	const float cz = fmaf(a.x, b.y, -a.y * b.x);
+	const float A2 = fmaf(cx, cx, fmaf(cy, cy, cz * cz));
+	const float dt = (b.t - a.t) + (b.te - a.te);
+	const float r = fmaf(-dt, dt, e2);
+	const float delta = fmaf(a1, dt, sqrt_a(A2 * fmaxf(r, 0.f))) * rcp_a(e2);
+	const float p = a.t + delta;
+	if(fmaf(a0, delta, q01 * dt) > 0.f && fmaf(a1, delta, -a.q * dt) > 0.f && !(r < 0.f) && p < best.p)
+		best = {p, a.t, delta, a.te};
+	if(!(A2 > 0.f) && distinct) best.p = -INFINITY;
+}
+
+// The triangle-by-triangle relaxation (reference order and degenerate rule),
+// for the rare star with a degenerate triangle.
+template <bool COH>
+__device__ __noinline__ float2 relax32_exact(const FieldDev &F, uint32_t v, const float2 *Do)
+{
+	uint32_t lab;
+	float2 vd;
+	bool skip;
+	return relax32<false, COH>(F, v, Do, nullptr, lab, 0u, false, vd, skip);
+}
+
+template <bool COH>
+__device__ __forceinline__ float2 relax32_lean(const FieldDev &F, uint32_t v, const float2 *Do, uint32_t win_s,
+                                               bool try_skip, float2 &vd, bool &skip)
+{
+	const unsigned am = __activemask();
+	const uint4 ra = __ldg(F.fan8 + 2 * (size_t) v), rb = __ldg(F.fan8 + 2 * (size_t) v + 1);
+	const float2 vs = ld2<COH>(Do + v);
+	vd = unflag(vs);
+	const float4 pv = __ldg(F.P + v);
+	const uint32_t u[FB] = {ra.x & FAN8_ID_MASK, ra.y, ra.z, ra.w, rb.x, rb.y, rb.z, rb.w};
+	const bool ovf = rb.w == FAN8_OVERFLOW;
+	const uint32_t n = (ra.x >> FAN8_N_SHIFT) & 15u;
+	// slots this lane walks: its row, plus the repeated first neighbour of a closed fan
+	const uint32_t m = ovf || n < 2 ? 0u : n + (ra.x >> 31);
+	const uint32_t mw = __reduce_max_sync(am, m);  // the warp walks mw slots
+	const unsigned live = __ballot_sync(am, m != 0);  // the lanes that go on below
+	if(ovf)
+	{
+		uint32_t lab;
+		return relax32_csr<false, COH>(F, v, Do, nullptr, lab, vd, pv);
+	}
+	if(!m) return vd;  // no triangle
+	if(try_skip && __all_sync(live, !flagged(vs.x)))
+	{
+		bool same = true;
+#pragma unroll
+		for(uint32_t k = 0; k < FB; k++)
+			if(k < mw) same &= u[k] >= win_s && !flagged(ld_d<float, COH>(reinterpret_cast<const float *>(Do + u[k])));
+		if(same)
+		{
+			skip = true;
+			return vd;
+		}
+	}
+	float bh = vd.x, bl = vd.y;
+	if(bh == INFINITY)
+	{
+		float mn = INFINITY;
+#pragma unroll
+		for(uint32_t k = 0; k < FB; k++)
+			if(k < mw) mn = fminf(mn, fabsf(ld2<COH>(Do + u[k]).x));
+		bh = mn == INFINITY ? 0.f : mn;
+		bl = 0.f;
+	}
+	const float old_rel = vd.x == INFINITY ? INFINITY : 0.f;
+	Best32 best = {old_rel, 0.f, 0.f, 0.f};
+	Nb32 last;
+	// slots in chunks of FC loaded together; the bound mw is the same on every
+	// lane, so the tests below are uniform branches
+#pragma unroll
+	for(uint32_t c = 0; c < FB; c += FC)
+	{
+		if(c >= mw) break;
+		float2 dk[FC];
+		float4 pk[FC];
+#pragma unroll
+		for(uint32_t q = 0; q < FC; q++)
+			if(q == 0 || c + q < mw)
+			{
+				dk[q] = ld2<COH>(Do + u[c + q]);
+				pk[q] = __ldg(F.P + u[c + q]);
+			}
+#pragma unroll
+		for(uint32_t q = 0; q < FC; q++)
+			if(q == 0 || c + q < mw)
+			{
+				const Nb32 cur = make_nb_lean(pk[q], rel_to_lean(unflag(dk[q]), bh, bl), pv);
+				take_edge(cur, best);
+				if(c + q > 0) take_planar(last, cur, u[c + q - 1] != u[c + q], best);
+				last = cur;
+			}
+	}
+	if(best.p == -INFINITY) return relax32_exact<COH>(F, v, Do);
+	if(!(best.p < old_rel)) return vd;
+	return df_result(bh, bl, {best.p, best.t, best.x, best.te});
+}
+
 // Relax window vertex v of field F (buffers d -> d^1) and, if v is in the
 // check ring (v < chk_e), apply relative_error + is_ok
 // (src/cuda/geodesics_ptp.cu:284-299, 371-375).  Returns 1 if v fails
@@ -527,7 +710,9 @@ __device__ __forceinline__ int sweep_vertex(const FieldDev &F, uint32_t d, uint3
 		const float2 *Do = static_cast<const float2 *>(F.D[d]);
 		float2 ov;
 		bool skip = false;
-		const float2 nv = relax32<CL, COH>(F, v, Do, Co, lab, win_s, try_skip, ov, skip);
+		float2 nv;
+		if constexpr(!CL && GP_LEAN) nv = relax32_lean<COH>(F, v, Do, win_s, try_skip, ov, skip);
+		else nv = relax32<CL, COH>(F, v, Do, Co, lab, win_s, try_skip, ov, skip);
 		if(skipped) *skipped = skip;
 		const bool chg = __float_as_uint(nv.x) != __float_as_uint(ov.x) || __float_as_uint(nv.y) != __float_as_uint(ov.y);
 		static_cast<float2 *>(F.D[d ^ 1u])[v] = make_float2(__uint_as_float(__float_as_uint(nv.x) | (chg ? 0x80000000u : 0u)), nv.y);
@@ -1455,9 +1640,12 @@ __global__ void fill_kernel(CatArgs c)
 					}
 					r[q] = x;
 				}
-				// the renumbered CSR fan: read by the FP64 sweeps, and by the FP32
-				// sweeps only for rows of more than 8 entries
-				if(sizeof(T) == 8 || n > 8)
+				// a row holds at most 8 entries, a closed one at most 7 (its first
+				// neighbour is repeated after the last, see below); longer rows are
+				// read from the renumbered CSR fan, which the FP64 sweeps always read
+				const bool cl = (o0f & FAN_CLOSED) != 0;
+				const bool ovf = n > 8 || (cl && n == 8);
+				if(sizeof(T) == 8 || ovf)
 					for(uint32_t e = o0; e < o1; e++)
 					{
 						const uint32_t q = e - o0;
@@ -1469,14 +1657,22 @@ __global__ void fill_kernel(CatArgs c)
 						}
 						F.fan[dst + q] = x;
 					}
-				if(n > 8) r[7] = FAN8_OVERFLOW;
+				// Padding: a closed fan repeats its first neighbour after its last
+				// (so the closing triangle is one more consecutive pair), and the
+				// slots after that repeat the row's last entry (pairs of one vertex,
+				// which the lean sweeps recognise by their equal ids).  Every slot
+				// of a row of 1-8 entries then names a real neighbour.
+				if(n && !ovf)
+				{
+					const uint32_t pad = cl ? r[0] : r[n - 1];
+					for(uint32_t q = n; q < 8; q++) r[q] = pad;
+				}
+				if(ovf) r[7] = FAN8_OVERFLOW;
 				// the star keeps the reference's triangle order (che::link from
 				// EVT), so the label rule's "first strictly smaller candidate"
 				// picks the same triangle as the reference in exact ties.  Slot 0
 				// packs closed | count | first neighbour (see FAN8_N_SHIFT)
-				r[0] = n ? (r[0] & FAN8_ID_MASK) | ((n <= 8 ? n : 0u) << FAN8_N_SHIFT) |
-				               ((o0f & FAN_CLOSED) ? FAN_CLOSED : 0u)
-				         : 0u;
+				r[0] = n ? (r[0] & FAN8_ID_MASK) | ((ovf ? 0u : n) << FAN8_N_SHIFT) | (cl ? FAN_CLOSED : 0u) : 0u;
 				F.fan8[2 * (size_t) k] = make_uint4(r[0], r[1], r[2], r[3]);
 				F.fan8[2 * (size_t) k + 1] = make_uint4(r[4], r[5], r[6], r[7]);
 			}
