@@ -87,6 +87,39 @@ __device__ __forceinline__ uint32_t discover(const FieldDev &F, uint32_t p, uint
 	return cand;
 }
 
+// discover for the one-CTA BFS (bfs_kernel): the same keys, but the visited
+// test reads ring[] through L1 instead of the keys through L2.  Only this CTA
+// writes the field's rings while its BFS runs (at emit time, ordered before
+// the next level by the CTA barrier), and a store from an SM updates that
+// SM's L1, so the cached ring of a vertex is current; many of a level's ring
+// loads hit lines the previous levels brought in.  A vertex met at this level
+// by a frontier position before ours may still get our atomic (its key is
+// not read first); the min keeps its key.  The rows of the vertices found are
+// prefetched into L1 for the next level, when they are the frontier.
+__device__ __forceinline__ uint32_t discover_local(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &ra,
+                                                   const uint4 &rb)
+{
+	if(rb.w == FAN8_OVERFLOW) return discover(F, p, v, ra, rb);
+	uint32_t r[8];
+#pragma unroll
+	for(uint32_t q = 0; q < 8; q++)
+	{
+		const uint32_t u = slot_of(ra, rb, q);
+		r[q] = u != FAN8_EMPTY ? __ldca(F.ring + u) : 0u;
+	}
+	uint32_t cand = 0;
+#pragma unroll
+	for(uint32_t q = 0; q < 8; q++)
+		if(r[q] == NIL)
+		{
+			const uint32_t u = slot_of(ra, rb, q);
+			atomicMin(F.key + u, (((unsigned long long) p << 20) | q) + 1);
+			asm volatile("prefetch.global.L1 [%0];" ::"l"(F.m.fan8 + 2 * (size_t) u));
+			cand |= 1u << q;
+		}
+	return cand;
+}
+
 // The vertices owned by frontier position p (key match), as a slot mask;
 // overflow rows report their count and are re-walked at emit time.
 __device__ __forceinline__ uint32_t owned(const FieldDev &F, uint32_t p, uint32_t v, const uint4 &ra, const uint4 &rb,
@@ -144,13 +177,13 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 					vv[c] = in_smem ? sf[cur][p - s] : ldcg(F.sorted + p);
 					ra[c] = __ldg(F.m.fan8 + 2 * (size_t) vv[c]);
 					rb[c] = __ldg(F.m.fan8 + 2 * (size_t) vv[c] + 1);
-					cm[c] = discover(F, p, vv[c], ra[c], rb[c]);
+					cm[c] = discover_local(F, p, vv[c], ra[c], rb[c]);
 				}
 			}
 			for(uint32_t p = s + SF + threadIdx.x; p < e; p += BT)
 			{
 				const uint32_t v = ldcg(F.sorted + p);
-				discover(F, p, v, __ldg(F.m.fan8 + 2 * (size_t) v), __ldg(F.m.fan8 + 2 * (size_t) v + 1));
+				discover_local(F, p, v, __ldg(F.m.fan8 + 2 * (size_t) v), __ldg(F.m.fan8 + 2 * (size_t) v + 1));
 			}
 			__syncthreads();
 			// pass 2: count, scan in frontier order (carried across chunks), emit
