@@ -355,6 +355,7 @@ def run_gpu(args, rank, world, local):
         "field_relax": field_relax, "gpu_dists": [dist32[voff[k]:voff[k + 1]] for k in range(F)],
         "plain_launches": sum(p.launches for p in pstats[-1]), "plain_steps": plain_steps,
         "grid_kernel": {0: "none", 1: "lockstep", 2: "queue"}.get(int(s0.grid_kernel), "?"),
+        "fields_streamed": int(s0.fields_streamed),
         "tuned": tuned, "graph": plan is not None, "launches_per_step": int(s0.launches),
         "strong": strong, "learned_over_reactive": learned_over_reactive,
     }
@@ -710,6 +711,7 @@ def main():
                    if res["ms_batched"] else None,
                    "parallelism": f"fields x{world}",
                    "schedule": args.schedule, "grid_kernel": res["grid_kernel"], "autotuned": res["tuned"],
+                   "fields_streamed": res["fields_streamed"],
                    "cuda_graph": res["graph"],
                    "l2": "inputs larger than L2 (129 MB): the step touches every mesh and field buffer"},
         "plain": {"value": plain, "unit": "fields/s", "ms_per_step": res["ms_plain"], "steps": res["plain_steps"],

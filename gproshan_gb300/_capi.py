@@ -46,7 +46,7 @@ class gp_ptp_opts(C.Structure):
                 ("threads", C.c_uint32), ("ctas", C.c_uint32), ("local_window", C.c_uint32),
                 ("round_coords", C.c_uint32), ("schedule", C.c_uint32), ("grid_kernel", C.c_uint32),
                 ("queue_min", C.c_uint32), ("queue_tile", C.c_uint32), ("normalize", C.c_uint32),
-                ("reserved2", C.c_uint32)]
+                ("stream_min", C.c_uint32)]
 
 
 class gp_ptp_stats(C.Structure):
@@ -57,7 +57,7 @@ class gp_ptp_stats(C.Structure):
 class gp_call_stats(C.Structure):
     _fields_ = [("launches", C.c_uint32), ("n_fields", C.c_uint32), ("fields_grid", C.c_uint32),
                 ("sweeps_grid", C.c_uint32), ("grid_kernel", C.c_uint32),
-                ("reserved", C.c_uint32), ("ms_toplesets", C.c_double), ("ms_renumber", C.c_double),
+                ("fields_streamed", C.c_uint32), ("ms_toplesets", C.c_double), ("ms_renumber", C.c_double),
                 ("ms_local", C.c_double), ("ms_grid", C.c_double), ("ms_gather", C.c_double),
                 ("relax_local", C.c_uint64), ("relax_grid", C.c_uint64), ("h2d_bytes", C.c_uint64),
                 ("d2h_bytes", C.c_uint64), ("skip_grid", C.c_uint64)]
@@ -351,8 +351,9 @@ GP_GRID_QUEUE = 2
 def make_opts(precision: int = GP_F32, max_iter: int = 0, tol: float = 0.0, ctas: int = 0,
               local_window: int = 0, round_coords: bool = False, schedule: int = GP_SCHED_REACTIVE,
               grid_kernel: int = GP_GRID_AUTO, queue_min: int = 0, queue_tile: int = 0,
-              normalize: bool = False) -> gp_ptp_opts:
+              normalize: bool = False, stream_min: int = 0) -> gp_ptp_opts:
     o = gp_ptp_opts()
+    o.stream_min = stream_min
     o.normalize = int(bool(normalize))
     o.queue_tile = queue_tile
     o.schedule = schedule
@@ -392,7 +393,7 @@ def ptp(mesh: DeviceMesh, sources, limits=None, sorted_=None, dtype=np.float32, 
 def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP_F32, ctas: int = 0,
               with_stats: bool = True, local_window: int = 0, round_coords: bool = False,
               schedule: int = GP_SCHED_REACTIVE, grid_kernel: int = GP_GRID_AUTO, queue_min: int = 0,
-              queue_tile: int = 0, clusters=None):
+              queue_tile: int = 0, clusters=None, stream_min: int = 0):
     """Solve many fields together (host arrays).  Returns (dists, stats, seconds).
     ``clusters``: optional list of per-field uint32 label arrays (initial labels
     in, labels out, updated in place)."""
@@ -420,7 +421,8 @@ def ptp_batch(ctx: Context, meshes, sources_list, dtype=np.float32, precision=GP
         fields[k].stats = C.addressof(stats[k]) if with_stats else None
     sec = C.c_double(0)
     opts = make_opts(precision, ctas=ctas, local_window=local_window, round_coords=round_coords,
-                     schedule=schedule, grid_kernel=grid_kernel, queue_min=queue_min, queue_tile=queue_tile)
+                     schedule=schedule, grid_kernel=grid_kernel, queue_min=queue_min, queue_tile=queue_tile,
+                     stream_min=stream_min)
     st = lib().gp_ptp_batch(ctx.handle, fields, n, C.byref(opts), out_t, 0, C.byref(sec))
     ctx.check(st, "gp_ptp_batch")
     return dists, stats, sec.value

@@ -46,7 +46,9 @@ cudaError_t launch_plan(const FieldDev *fields, const FieldState *state, uint32_
                         uint32_t local_window, uint32_t *pred_big, float *cost, uint32_t *perm, cudaStream_t s);
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
-                       const QCtl *ctl, uint32_t spin_limit, uint32_t phantom, cudaStream_t s);
+                       const QCtl *ctl, uint32_t spin_limit, uint32_t phantom, const uint32_t *sids,
+                       uint32_t n_stream, uint32_t workers, unsigned long long *sprog, unsigned long long *snap,
+                       cudaStream_t s);
 cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fields, QField *qf, QLine *cur,
                              QLine *done, QLine *sdone, QCtl *ctl, uint32_t ctas, uint32_t mode_req,
                              uint32_t min_queue, uint32_t tile, bool f64, bool clusters, cudaStream_t s);
@@ -218,6 +220,11 @@ constexpr uint32_t LOCAL_WINDOW_F32 = 4096u, LOCAL_WINDOW_F64 = 256u;
 // at a time, all CTAs); the others one CTA per field.
 constexpr uint32_t WIDE_MAX_FIELDS = 8;
 constexpr uint32_t WIDE_MIN_VERTICES = 1u << 18;
+// Streamed fields (FP32 distances, lockstep grid launch; gp_ptp_opts::stream_min):
+// fields on meshes of at least stream_min vertices build their toplesets inside
+// the sweep launch.  Off unless asked for: on the benchmark batch the streamed
+// launch hides the toplesets (9.3 -> 2.2 ms) but its sweeps run ~10 % slower.
+constexpr uint32_t STREAM_NEVER = 0xFFFFFFFFu;
 
 struct TopOut {  // host outputs of gp_toplesets
 	uint32_t *rings;
@@ -266,6 +273,27 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t tsz = 8;  // double (FP64 path) or a (hi, lo) float pair (FP32 path)
 	const size_t osz = out_type == GP_F64 ? sizeof(double) : sizeof(float);
 
+	// ---- streamed fields ------------------------------------------------------
+	// Streamed fields: the largest FP32 fields whose rows fit the padded fan
+	// rows, when the grid launch is the lockstep one (see stream_worker).
+	std::vector<uint32_t> sids;
+	const uint32_t smin = o.stream_min ? o.stream_min : STREAM_NEVER;
+	const bool lockstep = o.grid_kernel == GP_GRID_LOCKSTEP || (o.grid_kernel == GP_GRID_AUTO && !o.queue_min);
+	if(stage == Stage::ptp && !f64 && !clusters && !fps && !given_tops && lockstep && smin != STREAM_NEVER)
+	{
+		for(uint32_t f = 0; f < F; f++)
+			if(reqs[f].mesh && reqs[f].mesh->nv >= smin && reqs[f].mesh->dev.max_fan <= 7) sids.push_back(f);
+		std::stable_sort(sids.begin(), sids.end(),
+		                 [&](uint32_t x, uint32_t y) { return reqs[x].mesh->nv > reqs[y].mesh->nv; });
+		if(sids.size() > STREAM_MAX) sids.resize(STREAM_MAX);
+	}
+	const int maxc = stage == Stage::ptp ? ptp_max_ctas(ctx->device, f64, clusters, F) : 0;
+	const uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
+	// workers take at most a quarter of the launch's CTAs
+	while(!sids.empty() && (sids.size() + STREAM_PER_WORKER - 1) / STREAM_PER_WORKER > ctas / 4) sids.pop_back();
+	const uint32_t n_stream = (uint32_t) sids.size();
+	const uint32_t workers = (n_stream + STREAM_PER_WORKER - 1) / STREAM_PER_WORKER;
+
 	// ---- checks and layout -------------------------------------------------
 	std::vector<uint32_t> base(F + 1), vbase(F + 1), fbase(F + 1), sbase(F + 1);
 	uint64_t tot = 0, vtot = 0, ftot = 0, stot = 0;
@@ -295,6 +323,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 					set_err(ctx, "field %u: source %u = %u out of range (n_vertices %u)", f, s, r.src[s], nv);
 					return GP_ERR_INVALID_ARG;
 				}
+		if(n_stream) tot = align_up(tot, STREAM_MARGIN);  // no 128-byte line of a renumbered array spans two fields
 		base[f] = (uint32_t) tot;
 		vbase[f] = (uint32_t) vtot;
 		fbase[f] = (uint32_t) ftot;
@@ -346,6 +375,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 
 	Carve cv;
 	const size_t o_fields = cv.add<FieldDev>(F), o_state = cv.add<FieldState>(F);
+	const size_t o_sids = cv.add<uint32_t>(STREAM_MAX), o_sprog = cv.add<unsigned long long>(STREAM_MAX);
+	const size_t o_snap = cv.add<unsigned long long>(2 * STREAM_MAX);
 	const size_t o_sync = cv.add<GridSync>(2), o_base = cv.add<uint32_t>(F + 1), o_vbase = cv.add<uint32_t>(F + 1);
 	const size_t o_queue = cv.add<uint32_t>(4);
 	const size_t o_notok = cv.add<uint32_t>(3 * (size_t) F), o_bar = cv.add<uint32_t>(GRID_BAR_WORDS);
@@ -357,7 +388,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	std::vector<uint32_t> wide;
 	if(!given_tops && F <= WIDE_MAX_FIELDS && ctx->bfs_wide_ctas > 0)
 		for(uint32_t f = 0; f < F; f++)
-			if(reqs[f].mesh->nv >= WIDE_MIN_VERTICES) wide.push_back(f);
+			if(reqs[f].mesh->nv >= WIDE_MIN_VERTICES && std::find(sids.begin(), sids.end(), f) == sids.end())
+				wide.push_back(f);
 	const size_t o_wide = cv.add<uint32_t>(F), o_wbar = cv.add<uint32_t>(4);
 	const size_t o_wtot = cv.add<uint32_t>((size_t) std::max(ctx->bfs_wide_ctas, 1));
 	const size_t o_ring = cv.add<uint32_t>(tot), o_key = cv.add<unsigned long long>(tot);
@@ -447,6 +479,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		}
 		if(given_tops) hs[f].n_limits = r.nl;
 	}
+	for(uint32_t q = 0; q < n_stream; q++) hf[sids[q]].stream = q + 1;
 	// in-place label input and output on device pointers would race; stage them
 	if(clusters && out_dev)
 		for(uint32_t f = 0; f < F; f++)
@@ -473,6 +506,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	GP_CUDA(ctx, stage_copy(o_base, base.data(), 4 * (F + 1)));
 	GP_CUDA(ctx, stage_copy(o_vbase, vbase.data(), 4 * (F + 1)));
 	if(!wide.empty()) GP_CUDA(ctx, stage_copy(o_wide, wide.data(), 4 * wide.size()));
+	if(n_stream) GP_CUDA(ctx, stage_copy(o_sids, sids.data(), 4 * (size_t) n_stream));
 	if(fps)
 	{
 		// the seeds; the field's source count starts at n_init and grows on the device
@@ -527,7 +561,6 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		model = reinterpret_cast<const float *>(P(o_model));
 	}
 	const int kv = (f64 ? 2 : 0) + (clusters ? 1 : 0);
-	const int maxc = stage == Stage::ptp ? ptp_max_ctas(ctx->device, f64, clusters, F) : 0;
 	gp_call_stats cs{};
 	cs.n_fields = F;
 	auto record = [&](cudaEvent_t ev) { return plan ? cudaSuccess : cudaEventRecord(ev, s); };
@@ -581,18 +614,20 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		GP_CUDA(ctx, launch_ptp_local(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_queue)),
 		                              (uint32_t) ctx->local_ctas[kv], lw, perm, f64, clusters, s));
 		GP_CUDA(ctx, record(ctx->ph[3]));
-		uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
 		ctx->grid_ctas = ctas;
 		const uint32_t qmax = (uint32_t) ctx->queue_ctas[kv];
 		const uint32_t qctas = o.ctas ? std::min<uint32_t>(o.ctas, qmax) : qmax;
 		QCtl *dctl = reinterpret_cast<QCtl *>(P(o_qctl));
 		GP_CUDA(ctx, launch_ptp_queue(dF, dS, F, reinterpret_cast<QField *>(P(o_qf)), reinterpret_cast<QLine *>(P(o_qcur)),
 		                              reinterpret_cast<QLine *>(P(o_qdone)), reinterpret_cast<QLine *>(P(o_qsd)), dctl,
-		                              qctas, o.grid_kernel, o.queue_min ? o.queue_min : QUEUE_MIN_DEFAULT, o.queue_tile, f64,
-		                              clusters, s));
+		                              qctas, n_stream ? GP_GRID_LOCKSTEP : o.grid_kernel,
+		                              o.queue_min ? o.queue_min : QUEUE_MIN_DEFAULT, o.queue_tile, f64, clusters, s));
 		GP_CUDA(ctx, launch_ptp(dF, dS, F, reinterpret_cast<uint32_t *>(P(o_notok)),
 		                        reinterpret_cast<uint32_t *>(P(o_bar)), ctas, f64, clusters, ctx->steps,
-		                        ctx->steps_cap, dctl, ctx->dbg_spin, ctx->dbg_phantom, s));
+		                        ctx->steps_cap, dctl, ctx->dbg_spin, ctx->dbg_phantom,
+		                        reinterpret_cast<const uint32_t *>(P(o_sids)), n_stream, workers,
+		                        reinterpret_cast<unsigned long long *>(P(o_sprog)),
+		                        reinterpret_cast<unsigned long long *>(P(o_snap)), s));
 		GP_CUDA(ctx, record(ctx->ph[4]));
 		FpsDev *dfps = fps ? reinterpret_cast<FpsDev *>(P(o_fps)) : nullptr;
 		GP_CUDA(ctx, launch_gather_batch(dF, dS, dBase, F, (uint32_t) tot, f64, clusters, s,
@@ -753,6 +788,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		if(stage == Stage::ptp)
 			GP_CUDA(ctx, cudaMemcpy(hbar, P(o_bar), sizeof(hbar), cudaMemcpyDeviceToHost));
 		cs.grid_kernel = hctl.mode;
+		cs.fields_streamed = n_stream;
 		cs.sweeps_grid = hctl.mode == GRID_QUEUE ? hctl.progress : hbar[3];
 		cs.skip_grid = hctl.mode == GRID_QUEUE ? 0 : hbar[4] | (uint64_t) hbar[5] << 32;
 		cs.h2d_bytes = h2d;

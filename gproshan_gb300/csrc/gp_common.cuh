@@ -21,6 +21,18 @@ __device__ __forceinline__ uint32_t ld_acquire(const uint32_t *p)
 	return v;
 }
 
+__device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long *p)
+{
+	unsigned long long v;
+	asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+	return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned long long *p, unsigned long long v)
+{
+	asm volatile("st.release.gpu.global.u64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 __device__ __forceinline__ void st_release(uint32_t *p, uint32_t v)
 {
 	asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");

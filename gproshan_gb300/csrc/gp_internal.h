@@ -56,6 +56,11 @@ constexpr uint32_t QUEUE_STRIPES = 4;
 // abort, [2] error bits, [3] steps, then 16 group counters on 128-byte lines
 constexpr uint32_t GRID_BAR_WORDS = 32;  // one 128-byte line: see count_barrier
 constexpr uint32_t GRID_NONE = 0, GRID_LOCKSTEP = 1, GRID_QUEUE = 2;
+// Streamed fields (gp_ptp.cu, stream_worker): toplesets and renumbering built
+// by worker CTAs of the lockstep launch while the other CTAs sweep.
+constexpr uint32_t STREAM_MAX = 32;         // streamed fields per launch
+constexpr uint32_t STREAM_PER_WORKER = 4;   // fields one worker CTA interleaves
+constexpr uint32_t STREAM_MARGIN = 16;      // slots past a window's reads that must be final; field bases align to it
 
 struct alignas(128) QLine {
 	unsigned long long w;
@@ -133,6 +138,7 @@ struct FieldDev {
 	uint32_t round_coords;    // FP64 path on the float-rounded coordinates
 	double tol;
 	float tol32;              // tol rounded to float (the FP32 path's ring test)
+	uint32_t stream;          // 1: toplesets and renumbering run inside the lockstep launch (stream_*)
 };
 
 // Device-side state of a farthest-point sampling loop (gp_fps).

@@ -23,6 +23,7 @@
 #include <cmath>
 #include <type_traits>
 
+#include "gp_bfs.cuh"
 #include "gp_common.cuh"
 #include "gp_mlp.h"
 
@@ -293,9 +294,9 @@ __device__ __forceinline__ void open_sweep(const FieldDev &F, FieldState &st, bo
 	{
 		st.iter++;
 		if(st.i < (st.j >> 1)) st.i = st.j >> 1;
-		st.win_s = F.limits[st.i];
-		st.win_e = F.limits[st.j];
-		st.chk_e = F.limits[st.i + 1];
+		st.win_s = ldcg(F.limits + st.i);
+		st.win_e = ldcg(F.limits + st.j);
+		st.chk_e = ldcg(F.limits + st.i + 1);
 		st.live = 1;
 		if(trace && F.trace && st.n_iter < F.trace_cap)
 		{
@@ -765,6 +766,15 @@ __global__ void classify_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 		st.relax = 0;
 		st.max_iter = F.max_iter ? F.max_iter : (nl << 1);
 		st.n_limits = nl;
+		if(F.stream)
+		{
+			// toplesets still to come: the grid launch builds them, then opens
+			// the first window (n_limits, nr and max_iter are set there)
+			st.nr = 0;
+			st.big = 1;
+			st.live = 1;
+			return;
+		}
 		// a field the cost model expects to outgrow one CTA starts on the grid
 		// launch right away (its first sweep opened here)
 		if(pred_big && pred_big[warp] && nl >= 3)
@@ -939,6 +949,14 @@ struct GridArgs {
 	const QCtl *ctl;            // null, or the launch-mode choice (runs only if mode == GRID_LOCKSTEP)
 	uint32_t spin_limit;        // polls before a barrier wait gives up
 	uint32_t phantom;           // arrivals the barrier waits for beyond the launch's CTAs (0; tests)
+	// streamed fields (see stream_worker): their ids, the worker CTAs at the end
+	// of the launch, per-field progress words and the snapshot CTA 0 takes of them
+	const uint32_t *sids;
+	uint32_t n_stream;
+	uint32_t workers;
+	uint32_t ctas;              // sweeping CTAs: the launch's CTAs minus the workers
+	unsigned long long *sprog;  // n_stream, zeroed
+	unsigned long long *snap;   // 2 * STREAM_MAX
 };
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -949,6 +967,11 @@ __device__ __forceinline__ unsigned long long global_ns()
 }
 
 struct SchedSmem {
+	// live: bit 0 = a window is open this step; for a streamed field also bits
+	// 24-31 = its index in GridArgs::sids + 1, bits 8-9 = wait (1: the first
+	// window is not open yet, 2: a sweep is done and the next window waits for
+	// the rings it reads), bit 16 = that sweep's ring test passed.  (Packed: the
+	// entry stays 64 bytes, whose loads in the sweep loop are aligned.)
 	uint32_t i, j, d, iter, n_iter, max_iter, nl, live, win_s, win_e, chk_e;
 	// limits the next window may need, loaded while this step runs:
 	// [0..1] from i' = max(i, j'/2) (ring test failed), [2..3] from
@@ -956,12 +979,27 @@ struct SchedSmem {
 	uint32_t nx[5];
 };
 
+__device__ __forceinline__ uint32_t sched_sq(const SchedSmem &x) { return x.live >> 24; }  // 0: not streamed
+__device__ __forceinline__ uint32_t sched_wait(const SchedSmem &x) { return (x.live >> 8) & 3u; }
+
+template <bool STREAM>
 __device__ __forceinline__ void prefetch_limits(const FieldDev &F, SchedSmem &x)
 {
-	if(!x.live) return;
+	if(!(x.live & 1u)) return;
 	const uint32_t j1 = x.j < x.nl - 1 ? x.j + 1 : x.j;
 	const uint32_t ia = max(x.i, j1 >> 1), ib = max(x.i + 1, j1 >> 1);
 	const uint32_t *lim = F.limits;
+	if(STREAM && sched_sq(x))
+	{
+		// a streamed field's limits are written during this launch (L2 loads);
+		// x.nl is then a lower bound on its count, and every index below is known
+		x.nx[0] = ia < x.nl ? ldcg(lim + ia) : 0u;
+		x.nx[1] = ia + 1 < x.nl ? ldcg(lim + ia + 1) : 0u;
+		x.nx[2] = ib < x.nl ? ldcg(lim + ib) : 0u;
+		x.nx[3] = ib + 1 < x.nl ? ldcg(lim + ib + 1) : 0u;
+		x.nx[4] = ldcg(lim + j1);
+		return;
+	}
 	x.nx[0] = ia < x.nl ? lim[ia] : 0u;
 	x.nx[1] = ia + 1 < x.nl ? lim[ia + 1] : 0u;
 	x.nx[2] = ib < x.nl ? lim[ib] : 0u;
@@ -998,7 +1036,8 @@ __device__ __forceinline__ void open_sweep_cached(const FieldDev *F, FieldState 
 // up after `limit` polls (error bit set, abort raised, caller returns).
 // bar: [0] arrivals, [1] abort, [2] error bits, [3] steps, [4..5] skip count.
 
-__device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint32_t limit, uint32_t phantom)
+__device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint32_t limit, uint32_t phantom,
+                                              uint32_t ctas)
 {
 	__shared__ uint32_t s_ok;
 	__syncthreads();
@@ -1006,7 +1045,7 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint
 	{
 		s_ok = 1;
 		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
-		const uint32_t target = (gridDim.x + phantom) * (step + 1);
+		const uint32_t target = (ctas + phantom) * (step + 1);
 		uint32_t spins = 0;
 		while(ld_acquire(bar) < target)
 		{
@@ -1025,14 +1064,14 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint
 }
 
 // Tiles of every live window (TV window vertices per tile); ts[G] = total.
-template <uint32_t TV>
+template <uint32_t TV, bool STREAM>
 __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uint32_t G, uint32_t *s_tile)
 {
 	if(G <= NT)
 	{
 		// one round (the usual case): one block scan, the tile counter reset with it
 		const uint32_t q = threadIdx.x;
-		const uint32_t tiles = q < G && fs[q].live ? (fs[q].win_e - fs[q].win_s + TV - 1) / TV : 0u;
+		const uint32_t tiles = q < G && (STREAM ? (fs[q].live & 1u) : fs[q].live) ? (fs[q].win_e - fs[q].win_s + TV - 1) / TV : 0u;
 		uint32_t tot;
 		const uint32_t ex = block_exclusive_scan<NT>(tiles, &tot);
 		if(q < G) ts[q] = ex;
@@ -1054,7 +1093,7 @@ __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uin
 	for(uint32_t base = 0; base < G; base += NT)
 	{
 		const uint32_t q = base + threadIdx.x;
-		const uint32_t tiles = q < G && fs[q].live ? (fs[q].win_e - fs[q].win_s + TV - 1) / TV : 0u;
+		const uint32_t tiles = q < G && (STREAM ? (fs[q].live & 1u) : fs[q].live) ? (fs[q].win_e - fs[q].win_s + TV - 1) / TV : 0u;
 		uint32_t tot;
 		const uint32_t ex = block_exclusive_scan<NT>(tiles, &tot);
 		if(q < G) ts[q] = carry + ex;
@@ -1066,7 +1105,258 @@ __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uin
 	__syncthreads();
 }
 
-template <typename T, bool CL>
+// ---------------------------------------------------------------------------
+// Streamed fields: toplesets and ring renumbering inside the lockstep launch.
+//
+// The BFS of a field on a large mesh is a chain of levels (~5 us each on one
+// CTA: dependent L2 round trips and CTA barriers) as long as the field has
+// rings, and without streaming the field's sweeps start only after it ends.
+// But a sweep reads only the rings up to j + 1, and the sweeps advance about
+// one ring per grid step (tens of microseconds), far slower than the BFS.  So
+// the last `workers` CTAs of the launch build the toplesets of the streamed
+// fields -- up to STREAM_PER_WORKER each, one level of each in turn -- and
+// renumber every ring as soon as the next ring is known, publishing per field
+// the rings and positions done; the other CTAs sweep.  A streamed field opens
+// its next window only when the renumbered part covers every position the
+// window reads plus STREAM_MARGIN: the sweeps read positions and fan rows
+// through L1, which other SMs' writes do not update, so no 128-byte line a
+// sweep touches may still change (field bases are aligned to STREAM_MARGIN
+// slots for the same reason).  The readiness every sweeping CTA acts on is a
+// snapshot CTA 0 takes before it arrives at the step's barrier, so all copies
+// of the schedules take the same decisions; a field that waits just skips
+// steps.  The sweeps are the same sweeps in the same order as without
+// streaming, so the results are bit-identical.
+// ---------------------------------------------------------------------------
+constexpr uint32_t STREAM_DONE = 0x80000000u;  // progress: rings renumbered | DONE (high word), positions (low)
+constexpr unsigned long long STREAM_WAIT_NS = 2000000000ull;  // 2 s of steps without any window ready
+
+// Ring positions [k0, k1) of streamed field F: the FP32 sweeps' padded fan
+// rows, positions and initial distances, as fill_kernel writes them.
+__device__ __forceinline__ void stream_renumber(const FieldDev &F, uint32_t k0, uint32_t k1)
+{
+	float2 *D0 = static_cast<float2 *>(F.D[0]);
+	float2 *D1 = static_cast<float2 *>(F.D[1]);
+	for(uint32_t k = k0 + threadIdx.x; k < k1; k += NT)
+	{
+		const uint32_t v = ldcg(F.sorted + k);
+		const uint4 ra = __ldg(F.m.fan8 + 2 * (size_t) v), rb = __ldg(F.m.fan8 + 2 * (size_t) v + 1);
+		uint32_t r[8], n = 0;
+#pragma unroll
+		for(uint32_t q = 0; q < 8; q++)
+		{
+			const uint32_t u = slot_of(ra, rb, q);
+			r[q] = FAN8_EMPTY;
+			if(u != FAN8_EMPTY)
+			{
+				r[q] = ldcg(F.inv + u) - 1;  // every neighbour of a ring is in a ring already emitted
+				n = q + 1;
+			}
+		}
+		const bool cl = n && (ra.x & FAN_CLOSED);
+		if(n)
+		{
+			const uint32_t pad = cl ? r[0] : r[n - 1];
+#pragma unroll
+			for(uint32_t q = 1; q < 8; q++)
+				if(q >= n) r[q] = pad;
+		}
+		r[0] = n ? (r[0] & FAN8_ID_MASK) | (n << FAN8_N_SHIFT) | (cl ? FAN_CLOSED : 0u) : 0u;
+		F.fan8[2 * (size_t) k] = make_uint4(r[0], r[1], r[2], r[3]);
+		F.fan8[2 * (size_t) k + 1] = make_uint4(r[4], r[5], r[6], r[7]);
+		F.P[k] = __ldg(F.m.pos + v);
+		const float2 d0 = make_float2(k < F.ns ? 0.f : -INFINITY, 0.f);  // all but the sources flagged
+		D0[k] = d0;
+		D1[k] = d0;
+	}
+}
+
+// The sentinel slot nr (every unreached vertex reads it): no fan, distance INF.
+__device__ __forceinline__ void stream_sentinel(const FieldDev &F, uint32_t nr)
+{
+	F.fan8[2 * (size_t) nr] = make_uint4(0u, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);
+	F.fan8[2 * (size_t) nr + 1] = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);
+	F.P[nr] = make_float4(0.f, 0.f, 0.f, 0.f);
+	static_cast<float2 *>(F.D[0])[nr] = make_float2(INFINITY, 0.f);
+	static_cast<float2 *>(F.D[1])[nr] = make_float2(INFINITY, 0.f);
+}
+
+// One worker CTA: the toplesets of streamed fields w, w + workers, ... (the
+// one-CTA BFS of gp_toplesets.cu, same keys and order), one level of each in
+// turn; after level L (ring L + 1 emitted, with its new ids) ring L is
+// renumbered and the progress published (release): rings 0..L and positions
+// [0, limits[L + 1]).  The last level also writes the sentinel, n_limits and
+// nr, then publishes DONE.  Leaves early if the sweeping CTAs gave up.
+__device__ __noinline__ void stream_worker(const GridArgs &a, uint32_t w)
+{
+	// (no frontier copies in shared memory: any shared memory of this function
+	// is reserved on every SM of the launch and costs the sweeps L1 capacity)
+	__shared__ uint32_t wst[STREAM_PER_WORKER][4];  // level, s, e, live
+	__shared__ uint32_t s_abort;
+	const uint32_t W = a.workers;
+	uint32_t nf = 0;
+	for(uint32_t q = w; q < a.n_stream && nf < STREAM_PER_WORKER; q += W) nf++;
+	for(uint32_t t = 0; t < nf; t++)
+	{
+		const uint32_t f = a.sids[w + t * W];
+		const FieldDev &F = a.fields[f];
+		const bool live = a.state[f].bfs_live != 0;  // 0: a source outside the mesh (seed)
+		const uint32_t ns = live ? F.ns : 0u;
+		for(uint32_t k = threadIdx.x; k < ns; k += NT)
+			atomicMax(F.inv + ldcg(F.sorted + k), k + 1);  // repeated sources: the last occurrence
+		if(threadIdx.x == 0)
+		{
+			wst[t][0] = 0;
+			wst[t][1] = 0;
+			wst[t][2] = ns;
+			wst[t][3] = live;
+			if(!live)
+			{
+				// no toplesets: the gather reads the sentinel at slot 0
+				stream_sentinel(F, 0);
+				a.state[f].nr = 0;
+			}
+		}
+		__syncthreads();
+		if(!live && threadIdx.x == 0) st_release(a.sprog + w + t * W, (unsigned long long) STREAM_DONE << 32);
+	}
+	__syncthreads();
+	for(;;)
+	{
+		bool any = false;
+		for(uint32_t t = 0; t < nf; t++)
+		{
+			__syncthreads();
+			if(!wst[t][3]) continue;  // uniform: read after the barrier
+			any = true;
+			const uint32_t q = w + t * W, f = a.sids[q];
+			const FieldDev &F = a.fields[f];
+			const uint32_t level = wst[t][0], s = wst[t][1];
+			uint32_t e = wst[t][2];
+			// pass 1: discover (the first frontier chunk's rows kept in registers)
+			uint4 ra = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY), rb = ra;
+			uint32_t v0 = 0, c0 = 0;
+			if(s + threadIdx.x < e)
+			{
+				const uint32_t p = s + threadIdx.x;
+				v0 = ldcg(F.sorted + p);
+				ra = __ldg(F.m.fan8 + 2 * (size_t) v0);
+				rb = __ldg(F.m.fan8 + 2 * (size_t) v0 + 1);
+				c0 = discover_local(F, p, v0, ra, rb);
+			}
+			for(uint32_t p = s + NT + threadIdx.x; p < e; p += NT)
+			{
+				const uint32_t v = ldcg(F.sorted + p);
+				discover_local(F, p, v, __ldg(F.m.fan8 + 2 * (size_t) v), __ldg(F.m.fan8 + 2 * (size_t) v + 1));
+			}
+			__syncthreads();
+			// pass 2: count, scan in frontier order, emit with the new ids
+			uint32_t carry = 0;
+			for(uint32_t base = s, c = 0; base < e; base += NT, c++)
+			{
+				const uint32_t p = base + threadIdx.x;
+				uint32_t v = 0, cnt = 0, mask = 0, cand = 0xFFu;
+				uint4 x0 = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY), x1 = x0;
+				if(p < e)
+				{
+					if(c == 0)
+					{
+						v = v0;
+						x0 = ra;
+						x1 = rb;
+						cand = c0;
+					}
+					else
+					{
+						v = ldcg(F.sorted + p);
+						x0 = __ldg(F.m.fan8 + 2 * (size_t) v);
+						x1 = __ldg(F.m.fan8 + 2 * (size_t) v + 1);
+					}
+					mask = owned(F, p, v, x0, x1, cnt, cand);
+				}
+				uint32_t tot;
+				const uint32_t ex = block_exclusive_scan<NT>(cnt, &tot);
+				uint32_t o = carry + ex;
+#pragma unroll
+				for(uint32_t k = 0; k < 8; k++)
+					if(mask & (1u << k))
+					{
+						const uint32_t u = slot_of(x0, x1, k);
+						F.sorted[e + o] = u;
+						F.ring[u] = level + 1;
+						F.inv[u] = e + o + 1;
+						o++;
+					}
+				carry += tot;
+			}
+			__syncthreads();
+			// ring `level` = [s, e): all its neighbours have their new ids now
+			stream_renumber(F, s, e);
+			__syncthreads();
+			if(threadIdx.x == 0)
+			{
+				if(carry && e + carry > F.cap_sorted)
+				{
+					// more vertices than the field holds: a broken mesh table; end the
+					// field here (its sweeps see n_limits = 0) and report it
+					carry = 0;
+					e = 0;
+					a.state[f].status |= DEV_ERR_BOUNDS;
+					atomicOr(a.bar + 2, DEV_ERR_BOUNDS);
+				}
+				if(carry)
+				{
+					F.limits[level + 2] = e + carry;
+					wst[t][0] = level + 1;
+					wst[t][1] = e;
+					wst[t][2] = e + carry;
+					st_release(a.sprog + q, ((unsigned long long) (level + 1) << 32) | e);
+				}
+				else
+				{
+					stream_sentinel(F, e);
+					a.state[f].n_limits = e ? level + 2 : 0u;
+					a.state[f].nr = e;
+					a.state[f].bfs_live = 0;
+					wst[t][3] = 0;
+					st_release(a.sprog + q, ((unsigned long long) (STREAM_DONE | (level + 1)) << 32) | (e + 1));
+				}
+			}
+		}
+		if(threadIdx.x == 0) s_abort = ld_relaxed(a.bar + 1);  // the sweeping CTAs gave up
+		__syncthreads();
+		if(!any || s_abort) break;
+	}
+}
+
+// A streamed field at a step boundary (every sweeping CTA, same snapshot):
+// takes the ring test of a sweep just done, then returns -2 if the next
+// window still waits for its rings, -1 if the field is retired (or has no
+// sweep at all), 1 to open its first window, 0 to close and open as usual.
+__device__ __forceinline__ int stream_boundary(const GridArgs &a, SchedSmem &x, uint32_t f, const uint32_t *flags,
+                                            uint32_t step, bool *passed)
+{
+	if(!(x.live & 1u) && !sched_wait(x)) return -1;  // retired
+	if(x.live & 1u)
+		x.live = (x.live & 0xFF000000u) | (2u << 8) | (ldcg(flags + f) ? 0u : 1u << 16);
+	// ready: rings up to j + 1 renumbered, and the positions every window
+	// after this boundary reads (below limits[j + 2]) plus the margin
+	const unsigned long long pr = ldcg(a.snap + (step & 1) * STREAM_MAX + sched_sq(x) - 1);
+	const uint32_t rn = (uint32_t) (pr >> 32) & ~STREAM_DONE;
+	const bool done = ((pr >> 32) & STREAM_DONE) != 0;
+	const FieldDev &Fd = a.fields[f];
+	bool ready = done;
+	if(!done && rn >= x.j + 2) ready = (uint32_t) pr >= ldcg(Fd.limits + x.j + 2) + STREAM_MARGIN;
+	if(!ready) return -2;
+	x.nl = done ? ldcg(&a.state[f].n_limits) : rn + 1;
+	x.max_iter = Fd.max_iter ? Fd.max_iter : x.nl << 1;
+	const uint32_t w = sched_wait(x);
+	*passed = (x.live >> 16) & 1u;
+	x.live &= 0xFF000000u;  // neither open nor waiting (open_sweep sets bit 0 again)
+	if(x.nl < 3) return -1;  // no sweep (the reference's loop needs three limits)
+	return w == 1 ? 1 : 0;
+}
+
+template <typename T, bool CL, bool STREAM>
 __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 {
 	extern __shared__ __align__(16) unsigned char smem[];
@@ -1074,6 +1364,14 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	// compacted: entry q describes field id[q]; only fields handed to the grid.
 	// Layout: 8-byte counters first, then 4-byte-aligned arrays.
 	if(a.ctl && a.ctl->mode != GRID_LOCKSTEP) return;
+	if constexpr(STREAM)
+		if(blockIdx.x >= a.ctas)
+		{
+			stream_worker(a, blockIdx.x - a.ctas);
+			return;
+		}
+	// the sweeping CTAs: the whole launch, or (streaming) all but the workers
+	const uint32_t C = STREAM ? a.ctas : gridDim.x;
 	unsigned long long *rx = reinterpret_cast<unsigned long long *>(smem);
 	SchedSmem *fs = reinterpret_cast<SchedSmem *>(rx + F);
 	uint32_t *ts = reinterpret_cast<uint32_t *>(fs + F);
@@ -1084,6 +1382,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 
 	if(threadIdx.x == 0) s_G = 0;
 	__syncthreads();
+	bool waiting = false;  // (streaming) a streamed field waits for its rings
 	for(uint32_t base = 0; base < F; base += NT)
 	{
 		const uint32_t f = base + threadIdx.x;
@@ -1107,17 +1406,34 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			x.win_s = g.win_s;
 			x.win_e = g.win_e;
 			x.chk_e = g.chk_e;
+			if constexpr(STREAM)
+				if(a.fields[f].stream)
+				{
+					x.live = (a.fields[f].stream << 24) | (1u << 8);  // waits to open its first window
+					waiting = true;
+				}
 			rx[q] = g.relax;
 		}
 		__syncthreads();
 		if(threadIdx.x == 0) s_G += tot;
 		__syncthreads();
 	}
+	__shared__ uint32_t s_wait;                      // (streaming) kept out of the sweep loop's registers
+	__shared__ unsigned long long s_idle;            // (streaming) thread 0: start of a run of steps without tiles
+	if constexpr(STREAM)
+	{
+		waiting = __syncthreads_or(waiting);
+		if(threadIdx.x == 0)
+		{
+			s_wait = waiting;
+			s_idle = 0;
+		}
+	}
 	const uint32_t G = s_G;
 	__shared__ uint32_t s_tile;  // the CTA's next tile (see the step loop)
 	uint32_t n_skip = 0;  // this thread's relaxations skipped as unchanged (summed into bar[4..5] at the end)
-	grid_plan<TV>(fs, ts, G, &s_tile);
-	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
+	grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
+	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
 
 	for(uint32_t step = 0;; step++)
 	{
@@ -1125,19 +1441,31 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		if(blockIdx.x == 0 && threadIdx.x == 0 && a.steps && step < a.steps_cap)
 		{
 			uint32_t live = 0;
-			for(uint32_t q = 0; q < G; q++) live += fs[q].live;
+			for(uint32_t q = 0; q < G; q++) live += fs[q].live & 1u;
 			a.steps[2 * step] = global_ns();
 			a.steps[2 * step + 1] = ((unsigned long long) total << 32) | live;
 		}
-		if(!total)
+		if(!total && (!STREAM || !s_wait))
 		{
 			if(blockIdx.x == 0 && threadIdx.x == 0) a.bar[3] = step;
 			const uint32_t w = __reduce_add_sync(0xffffffffu, n_skip);
 			if(lane == 0 && w) atomicAdd(reinterpret_cast<unsigned long long *>(a.bar + 4), (unsigned long long) w);
 			break;
 		}
+		if constexpr(STREAM)
+			if(threadIdx.x == 0)
+			{
+				// steps without tiles only while streamed fields wait for rings: bounded
+				if(total) s_idle = 0;
+				else if(!s_idle) s_idle = global_ns();
+				else if(global_ns() - s_idle > STREAM_WAIT_NS)
+				{
+					atomicOr(a.bar + 2, DEV_ERR_TIMEOUT);
+					atomicExch(a.bar + 1, 1u);
+				}
+			}
 		uint32_t *flags = a.notok + (step % 3) * F;
-		const bool heavy = total >= gridDim.x * (NT / 32);  // see unflag: skip only in throughput-bound steps
+		const bool heavy = total >= C * (NT / 32);  // see unflag: skip only in throughput-bound steps
 		uint32_t lo = 0;  // entry of the warp's current tile; tiles only move forward
 		// CTA b (one per SM) owns tiles b, b + C, b + 2C, ...; its 32 warps take
 		// them in order from a shared counter (reset by grid_plan), so they all
@@ -1149,7 +1477,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			uint32_t r = 0;
 			if(lane == 0) r = atomicAdd(&s_tile, 1u);
 			r = __shfl_sync(0xffffffffu, r, 0);
-			const uint32_t k = blockIdx.x + r * gridDim.x;
+			const uint32_t k = blockIdx.x + r * C;
 			if(k >= total) break;
 			// last entry whose first tile <= k: the lanes test 32 entries at once
 			for(;;)
@@ -1170,14 +1498,34 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			// one atomic per warp that saw a failure, no block barrier per tile
 			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
 		}
-		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom)) return;
+		// (streaming) the workers' progress every CTA acts on at this boundary
+		if constexpr(STREAM)
+			if(blockIdx.x == 0 && threadIdx.x < a.n_stream)
+				a.snap[(step & 1) * STREAM_MAX + threadIdx.x] = ld_acquire(a.sprog + threadIdx.x);
+		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom, C)) return;
 		// every CTA advances its own copy of every schedule
+		bool wait_now = false;
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
 		{
 			SchedSmem &x = fs[q];
 			const uint32_t f = id[q];
 			if(blockIdx.x == 0) a.notok[((step + 2) % 3) * F + f] = 0;
-			if(!x.live) continue;
+			bool passed, open_first = false;
+			if(STREAM && sched_sq(x))
+			{
+				const int r = stream_boundary(a, x, f, flags, step, &passed);
+				if(r < 0)
+				{
+					wait_now |= r == -2;
+					continue;
+				}
+				open_first = r == 1;
+			}
+			else
+			{
+				if(!x.live) continue;
+				passed = !ldcg(flags + f);
+			}
 			FieldState st = {};
 			st.i = x.i;
 			st.j = x.j;
@@ -1189,23 +1537,31 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			st.win_s = x.win_s;
 			st.win_e = x.win_e;
 			st.relax = rx[q];
-			const bool passed = !ldcg(flags + f);
-			close_sweep(st, passed);
-			open_sweep_cached(blockIdx.x == 0 ? a.fields + f : nullptr, st, x, passed);
+			if(STREAM && open_first) open_sweep(a.fields[f], st, blockIdx.x == 0);
+			else
+			{
+				close_sweep(st, passed);
+				open_sweep_cached(blockIdx.x == 0 ? a.fields + f : nullptr, st, x, passed);
+			}
 			x.i = st.i;
 			x.j = st.j;
 			x.d = st.d;
 			x.iter = st.iter;
 			x.n_iter = st.n_iter;
-			x.live = st.live;
+			x.live = STREAM ? (x.live & 0xFF000000u) | st.live : st.live;
 			x.win_s = st.win_s;
 			x.win_e = st.win_e;
 			x.chk_e = st.chk_e;
 			rx[q] = st.relax;
 		}
-		__syncthreads();
-		grid_plan<TV>(fs, ts, G, &s_tile);
-		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
+		if constexpr(STREAM)
+		{
+			const bool w_any = __syncthreads_or(wait_now);
+			if(threadIdx.x == 0) s_wait = w_any;
+		}
+		else __syncthreads();
+		grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
+		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
 	}
 	if(blockIdx.x == 0)
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
@@ -1581,6 +1937,7 @@ __global__ void inv_set_kernel(CatArgs c)
 		const uint32_t f = upper_index(c.base, c.n_fields, g);
 		const uint32_t k = g - c.base[f];
 		const FieldState &st = c.state[f];
+		if(c.fields[f].stream) continue;  // renumbered inside the sweep launch
 		const uint32_t nr = st.n_limits ? c.fields[f].limits[st.n_limits - 1] : 0;
 		if(k < nr) atomicMax(&c.fields[f].inv[c.fields[f].sorted[k]], k + 1);
 	}
@@ -1594,7 +1951,7 @@ __global__ void count_kernel(CatArgs c)
 		const uint32_t k = g - c.base[f];
 		const FieldDev &F = c.fields[f];
 		const FieldState &st = c.state[f];
-		const uint32_t nr = st.n_limits ? F.limits[st.n_limits - 1] : 0;
+		const uint32_t nr = st.n_limits && !F.stream ? F.limits[st.n_limits - 1] : 0;
 		uint32_t n = 0;
 		if(k < nr)
 		{
@@ -1613,6 +1970,7 @@ __global__ void fill_kernel(CatArgs c)
 		const uint32_t f = upper_index(c.base, c.n_fields, g);
 		const uint32_t k = g - c.base[f];
 		const FieldDev &F = c.fields[f];
+		if(F.stream) continue;  // renumbered inside the sweep launch
 		const FieldState &st = c.state[f];
 		const uint32_t nr = st.n_limits ? F.limits[st.n_limits - 1] : 0;
 		const uint32_t n0 = st.n_limits >= 2 ? F.limits[1] : nr;
@@ -1948,10 +2306,12 @@ cudaError_t launch_gather_batch(FieldDev *fields, FieldState *state, const uint3
 	return cudaGetLastError();
 }
 
-static const void *ptp_kernel_ptr(bool f64, bool clusters)
+static const void *ptp_kernel_ptr(bool f64, bool clusters, bool stream = false)
 {
-	if(f64) return clusters ? (const void *) ptp_kernel<double, true> : (const void *) ptp_kernel<double, false>;
-	return clusters ? (const void *) ptp_kernel<float, true> : (const void *) ptp_kernel<float, false>;
+	if(f64)
+		return clusters ? (const void *) ptp_kernel<double, true, false> : (const void *) ptp_kernel<double, false, false>;
+	if(clusters) return (const void *) ptp_kernel<float, true, false>;
+	return stream ? (const void *) ptp_kernel<float, false, true> : (const void *) ptp_kernel<float, false, false>;
 }
 
 // grid launches keep the schedules of up to this many fields in shared memory
@@ -1965,6 +2325,9 @@ int ptp_max_ctas(int device, bool f64, bool clusters, uint32_t n_fields)
 	cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, device);
 	const void *k = ptp_kernel_ptr(f64, clusters);
 	cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int) grid_smem_bytes(GRID_MAX_FIELDS));
+	if(!f64 && !clusters)
+		cudaFuncSetAttribute(ptp_kernel_ptr(false, false, true), cudaFuncAttributeMaxDynamicSharedMemorySize,
+		                     (int) grid_smem_bytes(GRID_MAX_FIELDS));
 	cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k, NT, grid_smem_bytes(std::max<uint32_t>(n_fields, 1)));
 	return nsm * per;
 }
@@ -2018,16 +2381,24 @@ int ptp_binary_version()
 // notok: 3 * n_fields words; bar: 4 words.  Both zeroed here.
 cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *notok, uint32_t *bar,
                        uint32_t ctas, bool f64, bool clusters, unsigned long long *steps, uint32_t steps_cap,
-                       const QCtl *ctl, uint32_t spin_limit, uint32_t phantom, cudaStream_t s)
+                       const QCtl *ctl, uint32_t spin_limit, uint32_t phantom, const uint32_t *sids,
+                       uint32_t n_stream, uint32_t workers, unsigned long long *sprog, unsigned long long *snap,
+                       cudaStream_t s)
 {
 	if(!n_fields) return cudaSuccess;
+	if(n_stream && (f64 || clusters || n_stream > STREAM_MAX || !workers || workers >= ctas ||
+	                n_stream > workers * STREAM_PER_WORKER))
+		return cudaErrorInvalidValue;
 	cudaError_t e = cudaMemsetAsync(notok, 0, 3 * sizeof(uint32_t) * n_fields, s);
 	if(e == cudaSuccess) e = cudaMemsetAsync(bar, 0, GRID_BAR_WORDS * sizeof(uint32_t), s);
 	if(e == cudaSuccess && steps) e = cudaMemsetAsync(steps, 0, 16 * (size_t) steps_cap, s);
+	if(e == cudaSuccess && n_stream) e = cudaMemsetAsync(sprog, 0, sizeof(unsigned long long) * n_stream, s);
 	if(e != cudaSuccess) return e;
-	GridArgs a{fields, state, n_fields, notok, bar, steps, steps_cap, ctl, spin_limit ? spin_limit : SPIN_LIMIT, phantom};
+	const uint32_t w = n_stream ? workers : 0u;
+	GridArgs a{fields,  state, n_fields, notok, bar,      steps, steps_cap, ctl, spin_limit ? spin_limit : SPIN_LIMIT,
+	           phantom, sids,  n_stream, w,     ctas - w, sprog, snap};
 	void *args[] = {&a};
-	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters), dim3(ctas), dim3(NT), args,
+	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters, n_stream != 0), dim3(ctas), dim3(NT), args,
 	                                   grid_smem_bytes(n_fields), s);
 }
 

@@ -137,7 +137,11 @@ typedef struct gp_ptp_opts {
 	                          264-276; geodesics::normalize, src/geodesics.cpp:78-90),
 	                          on the device before any copy out: the maximum is
 	                          reduced inside the output gather */
-	uint32_t reserved2;
+	uint32_t stream_min;   /* GP_F32 without labels, lockstep grid launch: fields on meshes
+	                          of at least this many vertices (and at most 7 fan entries
+	                          per vertex) build their toplesets inside the sweep launch,
+	                          whose sweeps start as soon as the first rings are ready;
+	                          same results.  0 or 0xFFFFFFFF: never (the default) */
 } gp_ptp_opts;
 
 /* Grid-wide sweeps of the fields that outgrow one CTA.  LOCKSTEP: one
@@ -217,7 +221,7 @@ typedef struct gp_call_stats {
 	uint32_t fields_grid;      /* fields swept by the grid-wide launch */
 	uint32_t sweeps_grid;      /* steps of the lockstep launch, or sweeps completed by the queue launch */
 	uint32_t grid_kernel;      /* GP_GRID_LOCKSTEP, GP_GRID_QUEUE, or 0 if no field reached it */
-	uint32_t reserved;
+	uint32_t fields_streamed;  /* fields whose toplesets the lockstep launch built (gp_ptp_opts::stream_min) */
 	double ms_toplesets;       /* BFS setup + BFS */
 	double ms_renumber;        /* ring renumbering passes */
 	double ms_local;           /* classify + one-CTA-per-field sweeps */

@@ -1,0 +1,102 @@
+"""Toplesets built inside the lockstep sweep launch (gp_ptp_opts.stream_min).
+
+Worker CTAs of the grid-wide launch build the BFS and the ring renumbering of
+the streamed fields while the other CTAs sweep; a streamed field opens each
+window once the rings it reads are renumbered.  The sweeps are the same sweeps
+in the same order, so every output -- distances, sweep counts, relaxations --
+equals bit for bit the launch that builds every field's toplesets first
+(stream_min = 0xFFFFFFFF), and the FP32 bar against the FP64 oracle holds.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_cases
+
+pytestmark = pytest.mark.gpu
+
+NEVER = 0xFFFFFFFF
+REL_TOL_F32 = 1e-5
+
+
+def _run(ctx, ms, srcs, stream_min, **kw):
+    from gproshan_gb300 import _capi
+    d, st, _ = _capi.ptp_batch(ctx, ms, srcs, grid_kernel=_capi.GP_GRID_LOCKSTEP, stream_min=stream_min, **kw)
+    return d, [(s.n_iter, s.relaxations) for s in st], ctx.call_stats()
+
+
+def _meshes(ctx):
+    from gproshan_gb300 import _capi, meshgen
+    gen = [meshgen.icosphere(5, 0.1, 3), meshgen.height_field(200, 8), meshgen.height_field(8, 5, cols=900),
+           meshgen.torus(80, 200, seed=1), meshgen.icosphere(3, 0.1, 1)]
+    gen += [(g["xyz"], g["tri"]) for n, g in golden_cases() if n in ("grid_hole", "two_components", "grid24")]
+    return gen, [_capi.DeviceMesh(ctx, x, t) for x, t in gen]
+
+
+@pytest.mark.parametrize("stream_min,local_window", [(1, 1), (1, 0), (3000, 1)])
+def test_streamed_fields_bit_identical(gpu_ctx, oracle_lib, stream_min, local_window):
+    gen, dms = _meshes(gpu_ctx)
+    rng = np.random.default_rng(11 + stream_min)
+    ms, srcs, mi = [], [], []
+    for k in range(40):
+        q = k % len(dms)
+        ms.append(dms[q])
+        mi.append(q)
+        s = rng.choice(dms[q].n_vertices, size=1 + k % 3, replace=False)
+        if k % 7 == 3:
+            s = np.concatenate([s, s[:1]])  # a repeated source
+        srcs.append(s)
+    a, sa, ca = _run(gpu_ctx, ms, srcs, stream_min, local_window=local_window)
+    b, sb, cb = _run(gpu_ctx, ms, srcs, NEVER, local_window=local_window)
+    assert ca.fields_streamed > 0 and cb.fields_streamed == 0
+    assert sa == sb
+    for k in range(len(ms)):
+        assert np.array_equal(a[k], b[k]), k
+    for k in (0, 3, 5, 6, 7):  # icosphere, torus, mesh with a hole, two components (unreached vertices)
+        x, t = gen[mi[k]]
+        om = oracle_lib.Mesh(x, t)
+        ref = oracle_lib.ptp(om, srcs[k], xyz=x.astype(np.float32).astype(np.float64))
+        assert sa[k][0] == ref["n_iter"], k
+        assert oracle_lib.max_rel_err(a[k], ref["dist"]) <= REL_TOL_F32, k
+
+
+def test_single_streamed_field_and_learned_schedule(gpu_ctx):
+    """One large field alone (one worker CTA, the rest sweeping), and a batch
+    under the learned schedule: same bits as without streaming."""
+    from gproshan_gb300 import _capi, learned, meshgen
+    m = _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(400, 3))
+    for src in ([0], [12345, 160000 - 1]):
+        a, sa, ca = _run(gpu_ctx, [m], [src], 1)
+        b, sb, _ = _run(gpu_ctx, [m], [src], NEVER)
+        assert ca.fields_streamed == 1 and sa == sb and np.array_equal(a[0], b[0])
+    learned.install(gpu_ctx)
+    try:
+        _, dms = _meshes(gpu_ctx)
+        rng = np.random.default_rng(3)
+        ms = [dms[k % len(dms)] for k in range(24)]
+        srcs = [rng.choice(x.n_vertices, size=1, replace=False) for x in ms]
+        a, sa, ca = _run(gpu_ctx, ms, srcs, 1, schedule=_capi.GP_SCHED_LEARNED)
+        b, sb, _ = _run(gpu_ctx, ms, srcs, NEVER, schedule=_capi.GP_SCHED_LEARNED)
+        assert ca.fields_streamed > 0 and sa == sb
+        assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    finally:
+        _capi.set_cost_model(gpu_ctx, None)
+
+
+def test_streaming_off_where_it_does_not_apply(gpu_ctx):
+    """The default (stream_min 0), labels, FP64 and the work-queue launch
+    stream nothing; a threshold streams only the meshes at or above it."""
+    from gproshan_gb300 import _capi, meshgen
+    small = _capi.DeviceMesh(gpu_ctx, *meshgen.icosphere(4, 0.1, 2))
+    _run(gpu_ctx, [small, small], [[0], [5]], 0)
+    assert gpu_ctx.call_stats().fields_streamed == 0
+    _capi.ptp_batch(gpu_ctx, [small], [[0]], grid_kernel=_capi.GP_GRID_QUEUE, queue_min=1, stream_min=1)
+    assert gpu_ctx.call_stats().fields_streamed == 0
+    _capi.ptp_batch(gpu_ctx, [small], [[0]], dtype=np.float64, precision=_capi.GP_F64, stream_min=1)
+    assert gpu_ctx.call_stats().fields_streamed == 0
+    _capi.ptp_batch(gpu_ctx, [small], [[0]], clusters=[np.zeros(small.n_vertices, np.uint32)], stream_min=1)
+    assert gpu_ctx.call_stats().fields_streamed == 0
+    big = _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(520, 1))
+    _run(gpu_ctx, [big, small], [[7], [0]], 0)
+    assert gpu_ctx.call_stats().fields_streamed == 0
+    _run(gpu_ctx, [big, small], [[7], [0]], 1 << 18)
+    assert gpu_ctx.call_stats().fields_streamed == 1
