@@ -100,3 +100,49 @@ def test_streaming_off_where_it_does_not_apply(gpu_ctx):
     assert gpu_ctx.call_stats().fields_streamed == 0
     _run(gpu_ctx, [big, small], [[7], [0]], 1 << 18)
     assert gpu_ctx.call_stats().fields_streamed == 1
+
+
+def test_streamed_plan_replays_bit_exact(gpu_ctx):
+    """A captured plan (CUDA graph) with streamed fields: every replay, with
+    sources rewritten in place between launches, gives the bits of the
+    unstreamed batched call, including a source outside the mesh, which the
+    device reports and which leaves that field empty."""
+    torch = pytest.importorskip("torch")
+    from gproshan_gb300 import _capi
+    _, dms = _meshes(gpu_ctx)
+    ms = [dms[k % len(dms)] for k in range(12)]
+    rng = np.random.default_rng(21)
+    srcs = [rng.choice(m.n_vertices, size=1 + k % 2, replace=False).astype(np.uint32) for k, m in enumerate(ms)]
+    soff = np.concatenate([[0], np.cumsum([len(s) for s in srcs])])
+    voff = np.concatenate([[0], np.cumsum([m.n_vertices for m in ms])])
+    src_dev = torch.from_numpy(np.concatenate(srcs).astype(np.int32)).cuda()
+    dist_dev = torch.empty(int(voff[-1]), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    sp, dp = src_dev.data_ptr(), dist_dev.data_ptr()
+    plan = _capi.Plan(gpu_ctx, ms, [(sp + 4 * int(soff[k]), len(srcs[k])) for k in range(len(ms))],
+                      [dp + 4 * int(voff[k]) for k in range(len(ms))],
+                      opts=_capi.make_opts(grid_kernel=_capi.GP_GRID_LOCKSTEP, stream_min=1))
+    try:
+        for rnd in range(3):
+            plan.launch()
+            st = plan.wait()
+            got = dist_dev.cpu().numpy()
+            ref, rst, _ = _capi.ptp_batch(gpu_ctx, ms, srcs, grid_kernel=_capi.GP_GRID_LOCKSTEP, stream_min=NEVER)
+            for k in range(len(ms)):
+                assert np.array_equal(got[voff[k]:voff[k + 1]], ref[k]), (rnd, k)
+                assert st[k].n_iter == rst[k].n_iter and st[k].relaxations == rst[k].relaxations
+            srcs = [rng.choice(m.n_vertices, size=len(s), replace=False).astype(np.uint32) for m, s in zip(ms, srcs)]
+            src_dev.copy_(torch.from_numpy(np.concatenate(srcs).astype(np.int32)))
+            torch.cuda.synchronize()
+        # a source outside the mesh in a streamed field: reported, the rest unaffected
+        bad = np.concatenate(srcs).astype(np.int64)
+        bad[0] = ms[0].n_vertices + 3
+        src_dev.copy_(torch.from_numpy(bad.astype(np.int32)))
+        torch.cuda.synchronize()
+        plan.launch()
+        with pytest.raises(_capi.GPError):
+            plan.wait()
+    finally:
+        plan.close()
+    d, _, _ = _capi.ptp(ms[1], srcs[1])  # the context still works
+    assert np.isfinite(d).any()
