@@ -982,24 +982,18 @@ struct SchedSmem {
 __device__ __forceinline__ uint32_t sched_sq(const SchedSmem &x) { return x.live >> 24; }  // 0: not streamed
 __device__ __forceinline__ uint32_t sched_wait(const SchedSmem &x) { return (x.live >> 8) & 3u; }
 
-template <bool STREAM>
+// The limits the next boundary may need, loaded while the step runs (plain
+// loads).  A streamed field's limits are written during the launch and may sit
+// stale in this SM's L1, so its entries here are never used: its windows open
+// through open_sweep, which loads from L2.  (An L2 load here for streamed
+// fields alone raised the sweep loop's spills: grid phase +10 %.)  The
+// indices stay below x.nl, a lower bound on a streamed field's count.
 __device__ __forceinline__ void prefetch_limits(const FieldDev &F, SchedSmem &x)
 {
 	if(!(x.live & 1u)) return;
 	const uint32_t j1 = x.j < x.nl - 1 ? x.j + 1 : x.j;
 	const uint32_t ia = max(x.i, j1 >> 1), ib = max(x.i + 1, j1 >> 1);
 	const uint32_t *lim = F.limits;
-	if(STREAM && sched_sq(x))
-	{
-		// a streamed field's limits are written during this launch (L2 loads);
-		// x.nl is then a lower bound on its count, and every index below is known
-		x.nx[0] = ia < x.nl ? ldcg(lim + ia) : 0u;
-		x.nx[1] = ia + 1 < x.nl ? ldcg(lim + ia + 1) : 0u;
-		x.nx[2] = ib < x.nl ? ldcg(lim + ib) : 0u;
-		x.nx[3] = ib + 1 < x.nl ? ldcg(lim + ib + 1) : 0u;
-		x.nx[4] = ldcg(lim + j1);
-		return;
-	}
 	x.nx[0] = ia < x.nl ? lim[ia] : 0u;
 	x.nx[1] = ia + 1 < x.nl ? lim[ia + 1] : 0u;
 	x.nx[2] = ib < x.nl ? lim[ib] : 0u;
@@ -1418,14 +1412,18 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		if(threadIdx.x == 0) s_G += tot;
 		__syncthreads();
 	}
-	__shared__ uint32_t s_wait;                      // (streaming) kept out of the sweep loop's registers
+	// (streaming) some streamed field waits for rings: set at the boundary of
+	// step s in [(s + 1) & 1], read at the top of step s + 1 (kept in shared
+	// memory, out of the sweep loop's registers)
+	__shared__ uint32_t s_wait[2];
 	__shared__ unsigned long long s_idle;            // (streaming) thread 0: start of a run of steps without tiles
 	if constexpr(STREAM)
 	{
 		waiting = __syncthreads_or(waiting);
 		if(threadIdx.x == 0)
 		{
-			s_wait = waiting;
+			s_wait[0] = waiting;
+			s_wait[1] = 0;
 			s_idle = 0;
 		}
 	}
@@ -1433,7 +1431,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	__shared__ uint32_t s_tile;  // the CTA's next tile (see the step loop)
 	uint32_t n_skip = 0;  // this thread's relaxations skipped as unchanged (summed into bar[4..5] at the end)
 	grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
-	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
+	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
 
 	for(uint32_t step = 0;; step++)
 	{
@@ -1445,7 +1443,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			a.steps[2 * step] = global_ns();
 			a.steps[2 * step + 1] = ((unsigned long long) total << 32) | live;
 		}
-		if(!total && (!STREAM || !s_wait))
+		if(!total && (!STREAM || !s_wait[step & 1]))
 		{
 			if(blockIdx.x == 0 && threadIdx.x == 0) a.bar[3] = step;
 			const uint32_t w = __reduce_add_sync(0xffffffffu, n_skip);
@@ -1455,6 +1453,8 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		if constexpr(STREAM)
 			if(threadIdx.x == 0)
 			{
+				// s_wait[(step - 1) & 1] was read at the top of the previous step
+				s_wait[(step + 1) & 1] = 0;
 				// steps without tiles only while streamed fields wait for rings: bounded
 				if(total) s_idle = 0;
 				else if(!s_idle) s_idle = global_ns();
@@ -1504,19 +1504,19 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 				a.snap[(step & 1) * STREAM_MAX + threadIdx.x] = ld_acquire(a.sprog + threadIdx.x);
 		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom, C)) return;
 		// every CTA advances its own copy of every schedule
-		bool wait_now = false;
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
 		{
 			SchedSmem &x = fs[q];
 			const uint32_t f = id[q];
 			if(blockIdx.x == 0) a.notok[((step + 2) % 3) * F + f] = 0;
 			bool passed, open_first = false;
-			if(STREAM && sched_sq(x))
+			const bool streamed = STREAM && sched_sq(x);
+			if(streamed)
 			{
 				const int r = stream_boundary(a, x, f, flags, step, &passed);
 				if(r < 0)
 				{
-					wait_now |= r == -2;
+					if(r == -2) s_wait[(step + 1) & 1] = 1;
 					continue;
 				}
 				open_first = r == 1;
@@ -1537,7 +1537,12 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			st.win_s = x.win_s;
 			st.win_e = x.win_e;
 			st.relax = rx[q];
-			if(STREAM && open_first) open_sweep(a.fields[f], st, blockIdx.x == 0);
+			if(streamed)
+			{
+				// limits through L2 (see prefetch_limits)
+				if(!open_first) close_sweep(st, passed);
+				open_sweep(a.fields[f], st, blockIdx.x == 0);
+			}
 			else
 			{
 				close_sweep(st, passed);
@@ -1554,14 +1559,9 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			x.chk_e = st.chk_e;
 			rx[q] = st.relax;
 		}
-		if constexpr(STREAM)
-		{
-			const bool w_any = __syncthreads_or(wait_now);
-			if(threadIdx.x == 0) s_wait = w_any;
-		}
-		else __syncthreads();
+		__syncthreads();
 		grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
-		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
+		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
 	}
 	if(blockIdx.x == 0)
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
