@@ -54,6 +54,7 @@ cudaError_t launch_ptp_queue(FieldDev *fields, FieldState *state, uint32_t n_fie
                              uint32_t min_queue, uint32_t tile, bool f64, bool clusters, cudaStream_t s);
 int ptp_queue_max_ctas(int device, bool f64, bool clusters);
 uint32_t ptp_grid_max_fields();
+size_t ptp_snap_words(uint32_t n_fields);
 int ptp_binary_version();
 } // namespace gp
 
@@ -222,9 +223,14 @@ constexpr uint32_t WIDE_MAX_FIELDS = 8;
 constexpr uint32_t WIDE_MIN_VERTICES = 1u << 18;
 // Streamed fields (FP32 distances, lockstep grid launch; gp_ptp_opts::stream_min):
 // fields on meshes of at least stream_min vertices build their toplesets inside
-// the sweep launch.  Off unless asked for: on the benchmark batch the streamed
-// launch hides the toplesets (9.3 -> 2.2 ms) but its sweeps run ~10 % slower.
+// the sweep launch.  By default (stream_min 0) STREAM_DEFAULT_MIN, but only in
+// calls whose large fields would otherwise build their toplesets on one CTA
+// each (more than WIDE_MAX_FIELDS fields, or no whole-GPU BFS): there the
+// streamed launch hides the toplesets (benchmark batch 89.7 -> 86.8 ms); a call
+// of a few large fields is faster with the whole-GPU BFS first (2048^2 grid,
+// one field: 65 ms, streamed 86 ms).
 constexpr uint32_t STREAM_NEVER = 0xFFFFFFFFu;
+constexpr uint32_t STREAM_DEFAULT_MIN = 1u << 18;
 
 struct TopOut {  // host outputs of gp_toplesets
 	uint32_t *rings;
@@ -277,7 +283,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	// Streamed fields: the largest FP32 fields whose rows fit the padded fan
 	// rows, when the grid launch is the lockstep one (see stream_worker).
 	std::vector<uint32_t> sids;
-	const uint32_t smin = o.stream_min ? o.stream_min : STREAM_NEVER;
+	const bool wide_bfs = F <= WIDE_MAX_FIELDS && ctx->bfs_wide_ctas > 0;
+	const uint32_t smin = o.stream_min ? o.stream_min : wide_bfs ? STREAM_NEVER : STREAM_DEFAULT_MIN;
 	const bool lockstep = o.grid_kernel == GP_GRID_LOCKSTEP || (o.grid_kernel == GP_GRID_AUTO && !o.queue_min);
 	if(stage == Stage::ptp && !f64 && !clusters && !fps && !given_tops && lockstep && smin != STREAM_NEVER)
 	{
@@ -323,7 +330,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 					set_err(ctx, "field %u: source %u = %u out of range (n_vertices %u)", f, s, r.src[s], nv);
 					return GP_ERR_INVALID_ARG;
 				}
-		if(n_stream) tot = align_up(tot, STREAM_MARGIN);  // no 128-byte line of a renumbered array spans two fields
+		// no 128-byte line of a renumbered array or of the limits spans two fields
+		if(n_stream) tot = align_up(tot, STREAM_ALIGN);
 		base[f] = (uint32_t) tot;
 		vbase[f] = (uint32_t) vtot;
 		fbase[f] = (uint32_t) ftot;
@@ -376,7 +384,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	Carve cv;
 	const size_t o_fields = cv.add<FieldDev>(F), o_state = cv.add<FieldState>(F);
 	const size_t o_sids = cv.add<uint32_t>(STREAM_MAX), o_sprog = cv.add<unsigned long long>(STREAM_MAX);
-	const size_t o_snap = cv.add<unsigned long long>(2 * STREAM_MAX);
+	const size_t o_snap = cv.add<unsigned long long>(ptp_snap_words(F));
 	const size_t o_sync = cv.add<GridSync>(2), o_base = cv.add<uint32_t>(F + 1), o_vbase = cv.add<uint32_t>(F + 1);
 	const size_t o_queue = cv.add<uint32_t>(4);
 	const size_t o_notok = cv.add<uint32_t>(3 * (size_t) F), o_bar = cv.add<uint32_t>(GRID_BAR_WORDS);
@@ -386,7 +394,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_qdone = cv.add<QLine>((size_t) F * QUEUE_STRIPES), o_qsd = cv.add<QLine>(F);
 	const size_t o_qctl = cv.add<QCtl>(1), o_model = cv.add<float>(MLP_NPARAM);
 	std::vector<uint32_t> wide;
-	if(!given_tops && F <= WIDE_MAX_FIELDS && ctx->bfs_wide_ctas > 0)
+	if(!given_tops && wide_bfs)
 		for(uint32_t f = 0; f < F; f++)
 			if(reqs[f].mesh->nv >= WIDE_MIN_VERTICES && std::find(sids.begin(), sids.end(), f) == sids.end())
 				wide.push_back(f);

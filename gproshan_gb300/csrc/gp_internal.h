@@ -59,8 +59,9 @@ constexpr uint32_t GRID_NONE = 0, GRID_LOCKSTEP = 1, GRID_QUEUE = 2;
 // Streamed fields (gp_ptp.cu, stream_worker): toplesets and renumbering built
 // by worker CTAs of the lockstep launch while the other CTAs sweep.
 constexpr uint32_t STREAM_MAX = 32;         // streamed fields per launch
-constexpr uint32_t STREAM_PER_WORKER = 4;   // fields one worker CTA interleaves
-constexpr uint32_t STREAM_MARGIN = 16;      // slots past a window's reads that must be final; field bases align to it
+constexpr uint32_t STREAM_PER_WORKER = 2;   // fields one worker CTA interleaves (1: same speed, twice the workers)
+constexpr uint32_t STREAM_MARGIN = 16;      // slots past a window's reads that must be final
+constexpr uint32_t STREAM_ALIGN = 32;       // field bases (slots) with streamed fields: 128 bytes of 32-bit entries
 
 struct alignas(128) QLine {
 	unsigned long long w;

@@ -956,7 +956,7 @@ struct GridArgs {
 	uint32_t workers;
 	uint32_t ctas;              // sweeping CTAs: the launch's CTAs minus the workers
 	unsigned long long *sprog;  // n_stream, zeroed
-	unsigned long long *snap;   // 2 * STREAM_MAX
+	unsigned long long *snap;   // ptp_snap_words(n_fields): see SNAP_DONE
 };
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -983,14 +983,17 @@ __device__ __forceinline__ uint32_t sched_sq(const SchedSmem &x) { return x.live
 __device__ __forceinline__ uint32_t sched_wait(const SchedSmem &x) { return (x.live >> 8) & 3u; }
 
 // The limits the next boundary may need, loaded while the step runs (plain
-// loads).  A streamed field's limits are written during the launch and may sit
-// stale in this SM's L1, so its entries here are never used: its windows open
-// through open_sweep, which loads from L2.  (An L2 load here for streamed
-// fields alone raised the sweep loop's spills: grid phase +10 %.)  The
-// indices stay below x.nl, a lower bound on a streamed field's count.
+// loads).  Not for a streamed field: its limits are written during the launch,
+// and a line of them in this SM's L1 could be stale; its windows open through
+// open_sweep, which loads from L2.  Once its toplesets are done it becomes a
+// plain field (stream_boundary), and from then on its lines, which no plain
+// load touched before (field bases are 128-byte aligned in such a launch),
+// come fresh from L2.  (An L2-load branch here instead raised the sweep
+// loop's spills: grid phase +10 %.)
+template <bool STREAM>
 __device__ __forceinline__ void prefetch_limits(const FieldDev &F, SchedSmem &x)
 {
-	if(!(x.live & 1u)) return;
+	if(!(x.live & 1u) || (STREAM && sched_sq(x))) return;
 	const uint32_t j1 = x.j < x.nl - 1 ? x.j + 1 : x.j;
 	const uint32_t ia = max(x.i, j1 >> 1), ib = max(x.i + 1, j1 >> 1);
 	const uint32_t *lim = F.limits;
@@ -1029,9 +1032,10 @@ __device__ __forceinline__ void open_sweep_cached(const FieldDev *F, FieldState 
 // one more L2 round trip per step, measured 2-13 % slower.)  Bounded: gives
 // up after `limit` polls (error bit set, abort raised, caller returns).
 // bar: [0] arrivals, [1] abort, [2] error bits, [3] steps, [4..5] skip count.
+// `late` CTAs (streaming: the workers) arrive too at every step after *sj.
 
 __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint32_t limit, uint32_t phantom,
-                                              uint32_t ctas)
+                                              uint32_t ctas, const uint32_t *sj = nullptr, uint32_t late = 0)
 {
 	__shared__ uint32_t s_ok;
 	__syncthreads();
@@ -1039,7 +1043,8 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint
 	{
 		s_ok = 1;
 		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
-		const uint32_t target = (ctas + phantom) * (step + 1);
+		uint32_t target = (ctas + phantom) * (step + 1);
+		if(sj && step > *sj) target += late * (step - *sj);
 		uint32_t spins = 0;
 		while(ld_acquire(bar) < target)
 		{
@@ -1114,15 +1119,29 @@ __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uin
 // its next window only when the renumbered part covers every position the
 // window reads plus STREAM_MARGIN: the sweeps read positions and fan rows
 // through L1, which other SMs' writes do not update, so no 128-byte line a
-// sweep touches may still change (field bases are aligned to STREAM_MARGIN
+// sweep touches may still change (field bases are aligned to STREAM_ALIGN
 // slots for the same reason).  The readiness every sweeping CTA acts on is a
 // snapshot CTA 0 takes before it arrives at the step's barrier, so all copies
 // of the schedules take the same decisions; a field that waits just skips
 // steps.  The sweeps are the same sweeps in the same order as without
-// streaming, so the results are bit-identical.
+// streaming, so the results are bit-identical.  Once every worker is done,
+// the workers join the sweeps: at the first boundary whose snapshot counts
+// them all, CTA 0 writes its copy of the schedules out (stream_handover), and
+// from the next step on the tiles are dealt over the whole launch and the
+// barrier counts the workers too; each worker loads that copy (stream_join)
+// and enters the step loop there.
 // ---------------------------------------------------------------------------
 constexpr uint32_t STREAM_DONE = 0x80000000u;  // progress: rings renumbered | DONE (high word), positions (low)
 constexpr unsigned long long STREAM_WAIT_NS = 2000000000ull;  // 2 s of steps without any window ready
+// GridArgs::snap: [0, 2 * STREAM_MAX) the progress snapshots of the two step
+// parities, then (zeroed before the launch) the workers done as CTA 0 saw them
+// at the barrier of a step of parity p ([SNAP_DONE + p]), the workers done
+// ([SNAP_WORKERS]), the hand-over word ([SNAP_HAND]: 0 = not yet, else the
+// number of schedules << 32 | the workers' first step, or HAND_END), then the
+// handed-over schedules: SchedSmem[G], relaxations[G], field ids[G] (32-bit words)
+constexpr uint32_t SNAP_DONE = 2 * STREAM_MAX, SNAP_WORKERS = SNAP_DONE + 2, SNAP_HAND = SNAP_DONE + 3;
+constexpr uint32_t SNAP_STATE = SNAP_DONE + 4, SNAP_CTL_WORDS = 4;
+constexpr unsigned long long HAND_END = ~0ull;  // the launch ended before the workers joined
 
 // Ring positions [k0, k1) of streamed field F: the FP32 sweeps' padded fan
 // rows, positions and initial distances, as fill_kernel writes them.
@@ -1345,9 +1364,102 @@ __device__ __forceinline__ int stream_boundary(const GridArgs &a, SchedSmem &x, 
 	x.max_iter = Fd.max_iter ? Fd.max_iter : x.nl << 1;
 	const uint32_t w = sched_wait(x);
 	*passed = (x.live >> 16) & 1u;
-	x.live &= 0xFF000000u;  // neither open nor waiting (open_sweep sets bit 0 again)
+	// neither open nor waiting (open_sweep sets bit 0 again); a field whose
+	// toplesets are done is a plain field from here on (every CTA decides this
+	// on the same snapshot)
+	x.live &= done ? 0u : 0xFF000000u;
 	if(x.nl < 3) return -1;  // no sweep (the reference's loop needs three limits)
 	return w == 1 ? 1 : 0;
+}
+
+// The lockstep kernel's shared-memory layout (dynamic part) for F fields.
+struct GridSmem {
+	unsigned long long *rx;  // relaxations of each schedule
+	SchedSmem *fs;           // the schedules
+	uint32_t *ts;            // first tile of each schedule, ts[G] = total
+	uint32_t *id;            // field of each schedule
+};
+__device__ __forceinline__ GridSmem grid_smem(uint32_t F)
+{
+	extern __shared__ __align__(16) unsigned char smem[];
+	GridSmem g;
+	g.rx = reinterpret_cast<unsigned long long *>(smem);
+	g.fs = reinterpret_cast<SchedSmem *>(g.rx + F);
+	g.ts = reinterpret_cast<uint32_t *>(g.fs + F);
+	g.id = g.ts + F + 1;
+	return g;
+}
+constexpr uint32_t SCHED_WORDS = sizeof(SchedSmem) / 4;
+
+// CTA 0 at the boundary of `step` (all its threads, after the boundary's
+// updates): writes its G schedules out and releases them for the workers,
+// who sweep from step + 1 on.
+__device__ __noinline__ void stream_handover(unsigned long long *snap, uint32_t F, uint32_t G, uint32_t step)
+{
+	const GridSmem g = grid_smem(F);
+	uint32_t *dst = reinterpret_cast<uint32_t *>(snap + SNAP_STATE);
+	const uint32_t *fw = reinterpret_cast<const uint32_t *>(g.fs), *rw = reinterpret_cast<const uint32_t *>(g.rx);
+	for(uint32_t k = threadIdx.x; k < SCHED_WORDS * G; k += NT) dst[k] = fw[k];
+	for(uint32_t k = threadIdx.x; k < 2 * G; k += NT) dst[SCHED_WORDS * G + k] = rw[k];
+	for(uint32_t k = threadIdx.x; k < G; k += NT) dst[(SCHED_WORDS + 2) * G + k] = g.id[k];
+	__syncthreads();
+	if(threadIdx.x == 0)
+	{
+		__threadfence();
+		st_release(snap + SNAP_HAND, ((unsigned long long) G << 32) | (step + 1));
+	}
+}
+
+// A worker whose fields are all done (all its threads): counts itself done,
+// waits for CTA 0's hand-over and loads the schedules into its shared memory.
+// Returns G << 32 | the first step to sweep, or 0 to leave: the launch ended
+// or gave up first.  Bounded: gives up (error bit, abort) only if no CTA
+// arrives at a barrier for STREAM_WAIT_NS.
+__device__ __noinline__ unsigned long long stream_join(unsigned long long *snap, uint32_t *bar, uint32_t F)
+{
+	__shared__ unsigned long long s_hand;
+	if(threadIdx.x == 0)
+	{
+		__threadfence();
+		atomicAdd(snap + SNAP_WORKERS, 1ull);
+		unsigned long long h = 0, t0 = global_ns();
+		uint32_t seen = ld_relaxed(bar);
+		for(uint32_t it = 1;; it++)
+		{
+			h = ld_acquire(snap + SNAP_HAND);
+			if(h || ld_relaxed(bar + 1)) break;
+			if((it & 63u) == 0)
+			{
+				const uint32_t b = ld_relaxed(bar);
+				const unsigned long long t = global_ns();
+				if(b != seen)
+				{
+					seen = b;
+					t0 = t;
+				}
+				else if(t - t0 > STREAM_WAIT_NS)
+				{
+					atomicOr(bar + 2, DEV_ERR_TIMEOUT);
+					atomicExch(bar + 1, 1u);
+					break;
+				}
+			}
+			__nanosleep(256);
+		}
+		s_hand = h;
+	}
+	__syncthreads();
+	const unsigned long long h = s_hand;
+	if(!h || h == HAND_END) return 0;
+	const uint32_t G = (uint32_t) (h >> 32);
+	const GridSmem g = grid_smem(F);
+	const uint32_t *src = reinterpret_cast<const uint32_t *>(snap + SNAP_STATE);
+	uint32_t *fw = reinterpret_cast<uint32_t *>(g.fs), *rw = reinterpret_cast<uint32_t *>(g.rx);
+	for(uint32_t k = threadIdx.x; k < SCHED_WORDS * G; k += NT) fw[k] = ldcg(src + k);
+	for(uint32_t k = threadIdx.x; k < 2 * G; k += NT) rw[k] = ldcg(src + SCHED_WORDS * G + k);
+	for(uint32_t k = threadIdx.x; k < G; k += NT) g.id[k] = ldcg(src + (SCHED_WORDS + 2) * G + k);
+	__syncthreads();
+	return h;
 }
 
 template <typename T, bool CL, bool STREAM>
@@ -1358,59 +1470,72 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	// compacted: entry q describes field id[q]; only fields handed to the grid.
 	// Layout: 8-byte counters first, then 4-byte-aligned arrays.
 	if(a.ctl && a.ctl->mode != GRID_LOCKSTEP) return;
-	if constexpr(STREAM)
-		if(blockIdx.x >= a.ctas)
-		{
-			stream_worker(a, blockIdx.x - a.ctas);
-			return;
-		}
-	// the sweeping CTAs: the whole launch, or (streaming) all but the workers
-	const uint32_t C = STREAM ? a.ctas : gridDim.x;
 	unsigned long long *rx = reinterpret_cast<unsigned long long *>(smem);
 	SchedSmem *fs = reinterpret_cast<SchedSmem *>(rx + F);
 	uint32_t *ts = reinterpret_cast<uint32_t *>(fs + F);
 	uint32_t *id = ts + F + 1;
 	__shared__ uint32_t s_G;
+	__shared__ uint32_t s_sj;  // (streaming) the workers sweep after this step; ~0u: not yet
 	const uint32_t lane = threadIdx.x & 31;
 	constexpr uint32_t TV = 32;  // window vertices per tile: one warp's worth
 
-	if(threadIdx.x == 0) s_G = 0;
-	__syncthreads();
-	bool waiting = false;  // (streaming) a streamed field waits for its rings
-	for(uint32_t base = 0; base < F; base += NT)
+	uint32_t step0 = 0;  // (streaming) a worker enters the step loop at a later step
+	if constexpr(STREAM)
 	{
-		const uint32_t f = base + threadIdx.x;
-		const bool on = f < F && a.state[f].big && a.state[f].live;
-		uint32_t tot;
-		const uint32_t ex = block_exclusive_scan<NT>(on ? 1u : 0u, &tot);
-		if(on)
+		if(threadIdx.x == 0) s_sj = ~0u;
+		if(blockIdx.x >= a.ctas)
 		{
-			const FieldState &g = a.state[f];
-			const uint32_t q = s_G + ex;
-			SchedSmem &x = fs[q];
-			id[q] = f;
-			x.live = 1;
-			x.i = g.i;
-			x.j = g.j;
-			x.d = g.d;
-			x.iter = g.iter;
-			x.n_iter = g.n_iter;
-			x.max_iter = g.max_iter;
-			x.nl = g.n_limits;
-			x.win_s = g.win_s;
-			x.win_e = g.win_e;
-			x.chk_e = g.chk_e;
-			if constexpr(STREAM)
-				if(a.fields[f].stream)
-				{
-					x.live = (a.fields[f].stream << 24) | (1u << 8);  // waits to open its first window
-					waiting = true;
-				}
-			rx[q] = g.relax;
+			stream_worker(a, blockIdx.x - a.ctas);
+			const unsigned long long h = stream_join(a.snap, a.bar, F);
+			if(!h) return;
+			step0 = (uint32_t) h;
+			if(threadIdx.x == 0)
+			{
+				s_G = (uint32_t) (h >> 32);
+				s_sj = step0 - 1;
+			}
 		}
+	}
+	bool waiting = false;  // (streaming) a streamed field waits for its rings
+	if(!step0)
+	{
+		if(threadIdx.x == 0) s_G = 0;
 		__syncthreads();
-		if(threadIdx.x == 0) s_G += tot;
-		__syncthreads();
+		for(uint32_t base = 0; base < F; base += NT)
+		{
+			const uint32_t f = base + threadIdx.x;
+			const bool on = f < F && a.state[f].big && a.state[f].live;
+			uint32_t tot;
+			const uint32_t ex = block_exclusive_scan<NT>(on ? 1u : 0u, &tot);
+			if(on)
+			{
+				const FieldState &g = a.state[f];
+				const uint32_t q = s_G + ex;
+				SchedSmem &x = fs[q];
+				id[q] = f;
+				x.live = 1;
+				x.i = g.i;
+				x.j = g.j;
+				x.d = g.d;
+				x.iter = g.iter;
+				x.n_iter = g.n_iter;
+				x.max_iter = g.max_iter;
+				x.nl = g.n_limits;
+				x.win_s = g.win_s;
+				x.win_e = g.win_e;
+				x.chk_e = g.chk_e;
+				if constexpr(STREAM)
+					if(a.fields[f].stream)
+					{
+						x.live = (a.fields[f].stream << 24) | (1u << 8);  // waits to open its first window
+						waiting = true;
+					}
+				rx[q] = g.relax;
+			}
+			__syncthreads();
+			if(threadIdx.x == 0) s_G += tot;
+			__syncthreads();
+		}
 	}
 	// (streaming) some streamed field waits for rings: set at the boundary of
 	// step s in [(s + 1) & 1], read at the top of step s + 1 (kept in shared
@@ -1431,11 +1556,16 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	__shared__ uint32_t s_tile;  // the CTA's next tile (see the step loop)
 	uint32_t n_skip = 0;  // this thread's relaxations skipped as unchanged (summed into bar[4..5] at the end)
 	grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
-	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
+	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
 
-	for(uint32_t step = 0;; step++)
+	// (a worker that joined starts after s_sj: read from shared memory here, as
+	// a register held from the branch above raised the sweep loop's spills)
+	for(uint32_t step = STREAM && blockIdx.x >= a.ctas ? s_sj + 1 : 0u;; step++)
 	{
 		const uint32_t total = ts[G];
+		// the sweeping CTAs: the whole launch, or (streaming) all but the workers
+		// until they join
+		const uint32_t C = STREAM && step <= s_sj ? a.ctas : gridDim.x;
 		if(blockIdx.x == 0 && threadIdx.x == 0 && a.steps && step < a.steps_cap)
 		{
 			uint32_t live = 0;
@@ -1445,7 +1575,11 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		}
 		if(!total && (!STREAM || !s_wait[step & 1]))
 		{
-			if(blockIdx.x == 0 && threadIdx.x == 0) a.bar[3] = step;
+			if(blockIdx.x == 0 && threadIdx.x == 0)
+			{
+				a.bar[3] = step;
+				if(STREAM && s_sj == ~0u) st_release(a.snap + SNAP_HAND, HAND_END);
+			}
 			const uint32_t w = __reduce_add_sync(0xffffffffu, n_skip);
 			if(lane == 0 && w) atomicAdd(reinterpret_cast<unsigned long long *>(a.bar + 4), (unsigned long long) w);
 			break;
@@ -1455,6 +1589,10 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			{
 				// s_wait[(step - 1) & 1] was read at the top of the previous step
 				s_wait[(step + 1) & 1] = 0;
+				// every worker done at the previous step's snapshot: the workers sweep
+				// after this step (C of this step is a.ctas either way, so the other
+				// threads' unordered reads of s_sj agree)
+				if(s_sj == ~0u && a.workers && ldcg(a.snap + SNAP_DONE + ((step - 1) & 1)) == a.workers) s_sj = step;
 				// steps without tiles only while streamed fields wait for rings: bounded
 				if(total) s_idle = 0;
 				else if(!s_idle) s_idle = global_ns();
@@ -1463,6 +1601,15 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 					atomicOr(a.bar + 2, DEV_ERR_TIMEOUT);
 					atomicExch(a.bar + 1, 1u);
 				}
+			}
+		// (streaming) the workers' progress every CTA acts on at this step's
+		// boundary: taken before CTA 0's tiles, so that its loads do not delay
+		// CTA 0's arrival at the barrier
+		if constexpr(STREAM)
+			if(blockIdx.x == 0 && threadIdx.x < a.n_stream)
+			{
+				a.snap[(step & 1) * STREAM_MAX + threadIdx.x] = ld_acquire(a.sprog + threadIdx.x);
+				if(threadIdx.x == 0) a.snap[SNAP_DONE + (step & 1)] = ld_acquire(a.snap + SNAP_WORKERS);
 			}
 		uint32_t *flags = a.notok + (step % 3) * F;
 		const bool heavy = total >= C * (NT / 32);  // see unflag: skip only in throughput-bound steps
@@ -1498,11 +1645,9 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			// one atomic per warp that saw a failure, no block barrier per tile
 			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
 		}
-		// (streaming) the workers' progress every CTA acts on at this boundary
-		if constexpr(STREAM)
-			if(blockIdx.x == 0 && threadIdx.x < a.n_stream)
-				a.snap[(step & 1) * STREAM_MAX + threadIdx.x] = ld_acquire(a.sprog + threadIdx.x);
-		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom, C)) return;
+		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom, STREAM ? a.ctas : gridDim.x,
+		                  STREAM ? &s_sj : nullptr, gridDim.x - a.ctas))
+			return;
 		// every CTA advances its own copy of every schedule
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
 		{
@@ -1560,8 +1705,10 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			rx[q] = st.relax;
 		}
 		__syncthreads();
+		if constexpr(STREAM)
+			if(s_sj == step && blockIdx.x == 0) stream_handover(a.snap, F, G, step);
 		grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
-		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits(a.fields[id[q]], fs[q]);
+		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
 	}
 	if(blockIdx.x == 0)
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
@@ -2393,6 +2540,8 @@ cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, u
 	if(e == cudaSuccess) e = cudaMemsetAsync(bar, 0, GRID_BAR_WORDS * sizeof(uint32_t), s);
 	if(e == cudaSuccess && steps) e = cudaMemsetAsync(steps, 0, 16 * (size_t) steps_cap, s);
 	if(e == cudaSuccess && n_stream) e = cudaMemsetAsync(sprog, 0, sizeof(unsigned long long) * n_stream, s);
+	if(e == cudaSuccess && n_stream)
+		e = cudaMemsetAsync(snap + SNAP_DONE, 0, sizeof(unsigned long long) * SNAP_CTL_WORDS, s);
 	if(e != cudaSuccess) return e;
 	const uint32_t w = n_stream ? workers : 0u;
 	GridArgs a{fields,  state, n_fields, notok, bar,      steps, steps_cap, ctl, spin_limit ? spin_limit : SPIN_LIMIT,
@@ -2400,6 +2549,13 @@ cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, u
 	void *args[] = {&a};
 	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters, n_stream != 0), dim3(ctas), dim3(NT), args,
 	                                   grid_smem_bytes(n_fields), s);
+}
+
+// 64-bit words of GridArgs::snap for n_fields fields (snapshots, hand-over
+// words and the handed-over schedules)
+size_t ptp_snap_words(uint32_t n_fields)
+{
+	return SNAP_STATE + ((size_t) (SCHED_WORDS + 3) * n_fields + 1) / 2;
 }
 
 static const void *ptp_local_ptr(bool f64, bool clusters)

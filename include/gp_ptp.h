@@ -141,7 +141,9 @@ typedef struct gp_ptp_opts {
 	                          of at least this many vertices (and at most 7 fan entries
 	                          per vertex) build their toplesets inside the sweep launch,
 	                          whose sweeps start as soon as the first rings are ready;
-	                          same results.  0 or 0xFFFFFFFF: never (the default) */
+	                          same results.  0: the default, 2^18 in calls of more than
+	                          8 fields, never in smaller calls (their large fields build
+	                          toplesets with the whole GPU first); 0xFFFFFFFF: never */
 } gp_ptp_opts;
 
 /* Grid-wide sweeps of the fields that outgrow one CTA.  LOCKSTEP: one

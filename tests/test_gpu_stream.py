@@ -102,6 +102,28 @@ def test_streaming_off_where_it_does_not_apply(gpu_ctx):
     assert gpu_ctx.call_stats().fields_streamed == 1
 
 
+def test_default_streams_large_fields_of_larger_calls(gpu_ctx):
+    """stream_min 0 (the default) streams the fields on meshes of at least
+    2^18 vertices once a call has more than 8 fields, and never in smaller
+    calls, whose large fields build their toplesets with the whole GPU; the
+    streamed launch's workers join the sweeps once their toplesets are done,
+    and every output equals the unstreamed call's."""
+    from gproshan_gb300 import _capi, meshgen
+    big = _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(520, 1))
+    big2 = _capi.DeviceMesh(gpu_ctx, *meshgen.torus(200, 1400, seed=2))
+    _, dms = _meshes(gpu_ctx)
+    rng = np.random.default_rng(5)
+    ms = [big, big2, big] + [dms[k % len(dms)] for k in range(9)]
+    srcs = [rng.choice(m.n_vertices, size=1 + k % 2, replace=False) for k, m in enumerate(ms)]
+    a, sa, ca = _run(gpu_ctx, ms, srcs, 0)
+    assert ca.fields_streamed == 3
+    b, sb, cb = _run(gpu_ctx, ms, srcs, NEVER)
+    assert cb.fields_streamed == 0 and sa == sb
+    assert all(np.array_equal(x, y) for x, y in zip(a, b))
+    _run(gpu_ctx, ms[:8], srcs[:8], 0)
+    assert gpu_ctx.call_stats().fields_streamed == 0
+
+
 def test_streamed_plan_replays_bit_exact(gpu_ctx):
     """A captured plan (CUDA graph) with streamed fields: every replay, with
     sources rewritten in place between launches, gives the bits of the
