@@ -193,8 +193,9 @@ def run_gpu(args, rank, world, local):
     tuned = None
     if args.autotune and args.grid_kernel == "auto":
         # the library's autotuner picks the one-CTA window and the grid launch
-        # for this workload (untimed; every candidate gives the same results)
-        opts = _capi.autotune(ctx, [dmesh[mi] for mi, _ in fields], [[s] for _, s in fields], opts=opts, reps=1)
+        # for this workload (untimed; every candidate gives the same results;
+        # best of 3 per candidate: the windows' times differ by ~1 %)
+        opts = _capi.autotune(ctx, [dmesh[mi] for mi, _ in fields], [[s] for _, s in fields], opts=opts, reps=3)
         tuned = {"local_window": opts.local_window, "grid_kernel": {1: "lockstep", 2: "queue"}[opts.grid_kernel],
                  "queue_tile": opts.queue_tile}
     sec = C.c_double()
@@ -479,7 +480,7 @@ def cpu_baseline_sample(meshes, fields, field_relax, gpu_dists, max_nv: int = 40
       which runs the same schedule) times the GPU-counted relaxations of all
       of that mesh's fields gives the mesh's CPU time; the few larger meshes
       take the rate of the largest sampled mesh of their family.
-    * oracle check: every field of those meshes (all four per mesh, 240 on
+    * oracle check: every field of those meshes (all four per mesh, 244 on
       the benchmark batch) on the oracle port (FP64, float-rounded
       coordinates): the GPU FP32 result against the GPU-returned buffer (max
       rel. error, sweep counts); on the timed fields also the port's
@@ -737,7 +738,9 @@ def main():
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "peak_kind": pkind,
                      "unit": "GB/s", "frac": achieved / peak, "traffic": traffic,
                      "bytes_per_relaxation": ALGO_BYTES_PER_RELAX, "relaxations_per_launch": krelax,
-                     "ms_per_launch": kms},
+                     "ms_per_launch": kms}
+        | ({"launch_also": f"builds the toplesets of the {res['fields_streamed']} streamed fields (their BFS "
+                           f"and renumbering bytes are not counted above)"} if res["fields_streamed"] else {}),
         "phases_ms": {k: statistics.mean(s[k] for s in st) for k in
                       ("ms_toplesets", "ms_renumber", "ms_local", "ms_grid", "ms_gather")},
         "cpu_baseline": cpu,
