@@ -124,6 +124,31 @@ def test_default_streams_large_fields_of_larger_calls(gpu_ctx):
     assert gpu_ctx.call_stats().fields_streamed == 0
 
 
+def test_streaming_launch_gives_up_cleanly(gpu_ctx):
+    """A grid barrier that cannot complete (test hook: one arrival more than
+    the launch has) with streamed fields in the launch: the sweeping CTAs give
+    up after their poll limit, the workers leave their BFS and their wait for
+    the hand-over on the abort flag, the call reports GP_ERR_DEVICE_TIMEOUT,
+    and the context then gives the unstreamed call's bits."""
+    from gproshan_gb300 import _capi, meshgen
+    big = _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(520, 1))
+    _, dms = _meshes(gpu_ctx)
+    ms = [big, big] + dms[:8]
+    srcs = [[7], [1000]] + [[0]] * 8
+    ref, rst, _ = _run(gpu_ctx, ms, srcs, NEVER)
+    L = _capi.lib()
+    gpu_ctx.check(L.gp_ctx_debug_barrier(gpu_ctx.handle, 4000, 1), "gp_ctx_debug_barrier")
+    try:
+        with pytest.raises(_capi.GPError) as e:
+            _run(gpu_ctx, ms, srcs, 1)
+        assert e.value.status == _capi.GP_ERR_DEVICE_TIMEOUT
+    finally:
+        gpu_ctx.check(L.gp_ctx_debug_barrier(gpu_ctx.handle, 0, 0), "gp_ctx_debug_barrier")
+    d, st, cs = _run(gpu_ctx, ms, srcs, 1)
+    assert cs.fields_streamed >= 2 and st == rst
+    assert all(np.array_equal(x, y) for x, y in zip(d, ref))
+
+
 def test_streamed_plan_replays_bit_exact(gpu_ctx):
     """A captured plan (CUDA graph) with streamed fields: every replay, with
     sources rewritten in place between launches, gives the bits of the
