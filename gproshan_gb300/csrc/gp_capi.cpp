@@ -759,10 +759,10 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	QCtl hctl{};
 	if(stage == Stage::ptp)
 	{
-		uint32_t gb[4];
+		uint32_t gb[GRID_BAR_WORDS];
 		GP_CUDA(ctx, cudaMemcpy(gb, P(o_bar), sizeof(gb), cudaMemcpyDeviceToHost));
 		GP_CUDA(ctx, cudaMemcpy(&hctl, P(o_qctl), sizeof(hctl), cudaMemcpyDeviceToHost));
-		ferr |= gb[2] | hctl.err;
+		ferr |= gb[2] | gb[BAR_RESUME + 2] | hctl.err;
 	}
 	if(!wide.empty())
 	{
@@ -792,13 +792,17 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			}
 			else cs.relax_local += hs[f].relax;
 		}
-		uint32_t hbar[6] = {0, 0, 0, 0, 0, 0};
+		uint32_t hbar[GRID_BAR_WORDS] = {};
 		if(stage == Stage::ptp)
 			GP_CUDA(ctx, cudaMemcpy(hbar, P(o_bar), sizeof(hbar), cudaMemcpyDeviceToHost));
 		cs.grid_kernel = hctl.mode;
 		cs.fields_streamed = n_stream;
-		cs.sweeps_grid = hctl.mode == GRID_QUEUE ? hctl.progress : hbar[3];
-		cs.skip_grid = hctl.mode == GRID_QUEUE ? 0 : hbar[4] | (uint64_t) hbar[5] << 32;
+		// a streaming launch and the launch that resumes after it count apart
+		const uint32_t *rb = hbar + BAR_RESUME;
+		cs.sweeps_grid = hctl.mode == GRID_QUEUE ? hctl.progress : hbar[3] + rb[3];
+		cs.skip_grid = hctl.mode == GRID_QUEUE
+		                   ? 0
+		                   : (hbar[4] | (uint64_t) hbar[5] << 32) + (rb[4] | (uint64_t) rb[5] << 32);
 		cs.h2d_bytes = h2d;
 		cs.d2h_bytes = d2h + (stage == Stage::ptp ? 2 * sizeof(hbar) + sizeof(hctl) : 0);
 		ctx->last = cs;
@@ -1495,14 +1499,14 @@ gp_status gp_plan_wait(gp_plan *plan, void *stream, gp_ptp_stats *stats)
 	const uint32_t F = plan->n_fields;
 	std::vector<FieldState> hs(F);
 	GridSync hsync[2];
-	uint32_t hbar[4];
+	uint32_t hbar[GRID_BAR_WORDS];
 	QCtl hctl{};
 	GP_CUDA(ctx, cudaMemcpyAsync(hs.data(), plan->state, sizeof(FieldState) * F, cudaMemcpyDeviceToHost, s));
 	GP_CUDA(ctx, cudaMemcpyAsync(hsync, plan->sync, sizeof(hsync), cudaMemcpyDeviceToHost, s));
 	GP_CUDA(ctx, cudaMemcpyAsync(hbar, plan->bar, sizeof(hbar), cudaMemcpyDeviceToHost, s));
 	GP_CUDA(ctx, cudaMemcpyAsync(&hctl, plan->ctl, sizeof(hctl), cudaMemcpyDeviceToHost, s));
 	GP_CUDA(ctx, cudaStreamSynchronize(s));
-	uint32_t err = hsync[0].err | hsync[1].err | hbar[2] | hctl.err;
+	uint32_t err = hsync[0].err | hsync[1].err | hbar[2] | hbar[BAR_RESUME + 2] | hctl.err;
 	for(uint32_t f = 0; f < F; f++)
 	{
 		err |= hs[f].status;

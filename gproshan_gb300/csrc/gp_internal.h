@@ -55,6 +55,9 @@ constexpr uint32_t QUEUE_STRIPES = 4;
 // words of the lockstep grid launch's barrier block: [0] top arrivals, [1]
 // abort, [2] error bits, [3] steps, then 16 group counters on 128-byte lines
 constexpr uint32_t GRID_BAR_WORDS = 32;  // one 128-byte line: see count_barrier
+// the barrier words of the launch that resumes after a streaming launch: the
+// line's second half (errors, steps and skip counts are read from both)
+constexpr uint32_t BAR_RESUME = GRID_BAR_WORDS / 2;
 constexpr uint32_t GRID_NONE = 0, GRID_LOCKSTEP = 1, GRID_QUEUE = 2;
 // Streamed fields (gp_ptp.cu, stream_worker): toplesets and renumbering built
 // by worker CTAs of the lockstep launch while the other CTAs sweep.

@@ -957,6 +957,9 @@ struct GridArgs {
 	uint32_t ctas;              // sweeping CTAs: the launch's CTAs minus the workers
 	unsigned long long *sprog;  // n_stream, zeroed
 	unsigned long long *snap;   // ptp_snap_words(n_fields): see SNAP_DONE
+	// a launch that resumes after a streaming launch: that launch's barrier
+	// words (nothing to do if it gave up; its step count offsets the trace)
+	const uint32_t *prev;
 };
 
 __device__ __forceinline__ unsigned long long global_ns()
@@ -1032,10 +1035,9 @@ __device__ __forceinline__ void open_sweep_cached(const FieldDev *F, FieldState 
 // one more L2 round trip per step, measured 2-13 % slower.)  Bounded: gives
 // up after `limit` polls (error bit set, abort raised, caller returns).
 // bar: [0] arrivals, [1] abort, [2] error bits, [3] steps, [4..5] skip count.
-// `late` CTAs (streaming: the workers) arrive too at every step after *sj.
 
 __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint32_t limit, uint32_t phantom,
-                                              uint32_t ctas, const uint32_t *sj = nullptr, uint32_t late = 0)
+                                              uint32_t ctas)
 {
 	__shared__ uint32_t s_ok;
 	__syncthreads();
@@ -1043,8 +1045,7 @@ __device__ __forceinline__ bool count_barrier(uint32_t *bar, uint32_t step, uint
 	{
 		s_ok = 1;
 		asm volatile("red.release.gpu.global.add.u32 [%0], 1;" ::"l"(bar) : "memory");
-		uint32_t target = (ctas + phantom) * (step + 1);
-		if(sj && step > *sj) target += late * (step - *sj);
+		const uint32_t target = (ctas + phantom) * (step + 1);
 		uint32_t spins = 0;
 		while(ld_acquire(bar) < target)
 		{
@@ -1124,24 +1125,20 @@ __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uin
 // snapshot CTA 0 takes before it arrives at the step's barrier, so all copies
 // of the schedules take the same decisions; a field that waits just skips
 // steps.  The sweeps are the same sweeps in the same order as without
-// streaming, so the results are bit-identical.  Once every worker is done,
-// the workers join the sweeps: at the first boundary whose snapshot counts
-// them all, CTA 0 writes its copy of the schedules out (stream_handover), and
-// from the next step on the tiles are dealt over the whole launch and the
-// barrier counts the workers too; each worker loads that copy (stream_join)
-// and enters the step loop there.
+// streaming, so the results are bit-identical.  Once every worker is done
+// (the first boundary whose snapshot counts them all), the launch writes every
+// schedule back to its FieldState and ends; a launch of the plain lockstep
+// kernel, which starts from the FieldState, sweeps the rest on every SM and
+// with the plain kernel's code.
 // ---------------------------------------------------------------------------
 constexpr uint32_t STREAM_DONE = 0x80000000u;  // progress: rings renumbered | DONE (high word), positions (low)
 constexpr unsigned long long STREAM_WAIT_NS = 2000000000ull;  // 2 s of steps without any window ready
 // GridArgs::snap: [0, 2 * STREAM_MAX) the progress snapshots of the two step
 // parities, then (zeroed before the launch) the workers done as CTA 0 saw them
-// at the barrier of a step of parity p ([SNAP_DONE + p]), the workers done
-// ([SNAP_WORKERS]), the hand-over word ([SNAP_HAND]: 0 = not yet, else the
-// number of schedules << 32 | the workers' first step, or HAND_END), then the
-// handed-over schedules: SchedSmem[G], relaxations[G], field ids[G] (32-bit words)
-constexpr uint32_t SNAP_DONE = 2 * STREAM_MAX, SNAP_WORKERS = SNAP_DONE + 2, SNAP_HAND = SNAP_DONE + 3;
-constexpr uint32_t SNAP_STATE = SNAP_DONE + 4, SNAP_CTL_WORDS = 4;
-constexpr unsigned long long HAND_END = ~0ull;  // the launch ended before the workers joined
+// at the start of a step of parity p ([SNAP_DONE + p]) and the workers done
+// ([SNAP_WORKERS]).
+constexpr uint32_t SNAP_DONE = 2 * STREAM_MAX, SNAP_WORKERS = SNAP_DONE + 2;
+constexpr uint32_t SNAP_WORDS = SNAP_DONE + 4, SNAP_CTL_WORDS = 4;
 
 // Ring positions [k0, k1) of streamed field F: the FP32 sweeps' padded fan
 // rows, positions and initial distances, as fill_kernel writes them.
@@ -1372,96 +1369,6 @@ __device__ __forceinline__ int stream_boundary(const GridArgs &a, SchedSmem &x, 
 	return w == 1 ? 1 : 0;
 }
 
-// The lockstep kernel's shared-memory layout (dynamic part) for F fields.
-struct GridSmem {
-	unsigned long long *rx;  // relaxations of each schedule
-	SchedSmem *fs;           // the schedules
-	uint32_t *ts;            // first tile of each schedule, ts[G] = total
-	uint32_t *id;            // field of each schedule
-};
-__device__ __forceinline__ GridSmem grid_smem(uint32_t F)
-{
-	extern __shared__ __align__(16) unsigned char smem[];
-	GridSmem g;
-	g.rx = reinterpret_cast<unsigned long long *>(smem);
-	g.fs = reinterpret_cast<SchedSmem *>(g.rx + F);
-	g.ts = reinterpret_cast<uint32_t *>(g.fs + F);
-	g.id = g.ts + F + 1;
-	return g;
-}
-constexpr uint32_t SCHED_WORDS = sizeof(SchedSmem) / 4;
-
-// CTA 0 at the boundary of `step` (all its threads, after the boundary's
-// updates): writes its G schedules out and releases them for the workers,
-// who sweep from step + 1 on.
-__device__ __noinline__ void stream_handover(unsigned long long *snap, uint32_t F, uint32_t G, uint32_t step)
-{
-	const GridSmem g = grid_smem(F);
-	uint32_t *dst = reinterpret_cast<uint32_t *>(snap + SNAP_STATE);
-	const uint32_t *fw = reinterpret_cast<const uint32_t *>(g.fs), *rw = reinterpret_cast<const uint32_t *>(g.rx);
-	for(uint32_t k = threadIdx.x; k < SCHED_WORDS * G; k += NT) dst[k] = fw[k];
-	for(uint32_t k = threadIdx.x; k < 2 * G; k += NT) dst[SCHED_WORDS * G + k] = rw[k];
-	for(uint32_t k = threadIdx.x; k < G; k += NT) dst[(SCHED_WORDS + 2) * G + k] = g.id[k];
-	__syncthreads();
-	if(threadIdx.x == 0)
-	{
-		__threadfence();
-		st_release(snap + SNAP_HAND, ((unsigned long long) G << 32) | (step + 1));
-	}
-}
-
-// A worker whose fields are all done (all its threads): counts itself done,
-// waits for CTA 0's hand-over and loads the schedules into its shared memory.
-// Returns G << 32 | the first step to sweep, or 0 to leave: the launch ended
-// or gave up first.  Bounded: gives up (error bit, abort) only if no CTA
-// arrives at a barrier for STREAM_WAIT_NS.
-__device__ __noinline__ unsigned long long stream_join(unsigned long long *snap, uint32_t *bar, uint32_t F)
-{
-	__shared__ unsigned long long s_hand;
-	if(threadIdx.x == 0)
-	{
-		__threadfence();
-		atomicAdd(snap + SNAP_WORKERS, 1ull);
-		unsigned long long h = 0, t0 = global_ns();
-		uint32_t seen = ld_relaxed(bar);
-		for(uint32_t it = 1;; it++)
-		{
-			h = ld_acquire(snap + SNAP_HAND);
-			if(h || ld_relaxed(bar + 1)) break;
-			if((it & 63u) == 0)
-			{
-				const uint32_t b = ld_relaxed(bar);
-				const unsigned long long t = global_ns();
-				if(b != seen)
-				{
-					seen = b;
-					t0 = t;
-				}
-				else if(t - t0 > STREAM_WAIT_NS)
-				{
-					atomicOr(bar + 2, DEV_ERR_TIMEOUT);
-					atomicExch(bar + 1, 1u);
-					break;
-				}
-			}
-			__nanosleep(256);
-		}
-		s_hand = h;
-	}
-	__syncthreads();
-	const unsigned long long h = s_hand;
-	if(!h || h == HAND_END) return 0;
-	const uint32_t G = (uint32_t) (h >> 32);
-	const GridSmem g = grid_smem(F);
-	const uint32_t *src = reinterpret_cast<const uint32_t *>(snap + SNAP_STATE);
-	uint32_t *fw = reinterpret_cast<uint32_t *>(g.fs), *rw = reinterpret_cast<uint32_t *>(g.rx);
-	for(uint32_t k = threadIdx.x; k < SCHED_WORDS * G; k += NT) fw[k] = ldcg(src + k);
-	for(uint32_t k = threadIdx.x; k < 2 * G; k += NT) rw[k] = ldcg(src + SCHED_WORDS * G + k);
-	for(uint32_t k = threadIdx.x; k < G; k += NT) g.id[k] = ldcg(src + (SCHED_WORDS + 2) * G + k);
-	__syncthreads();
-	return h;
-}
-
 template <typename T, bool CL, bool STREAM>
 __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 {
@@ -1470,72 +1377,70 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	// compacted: entry q describes field id[q]; only fields handed to the grid.
 	// Layout: 8-byte counters first, then 4-byte-aligned arrays.
 	if(a.ctl && a.ctl->mode != GRID_LOCKSTEP) return;
+	if(!STREAM && a.prev && ld_relaxed(a.prev + 1)) return;  // resuming after a launch that gave up
+	if constexpr(STREAM)
+		if(blockIdx.x >= a.ctas)
+		{
+			stream_worker(a, blockIdx.x - a.ctas);
+			if(threadIdx.x == 0)
+			{
+				__threadfence();
+				atomicAdd(a.snap + SNAP_WORKERS, 1ull);  // this worker's fields are all done
+			}
+			return;
+		}
+	// the sweeping CTAs: the whole launch, or (streaming) all but the workers
+	const uint32_t C = STREAM ? a.ctas : gridDim.x;
 	unsigned long long *rx = reinterpret_cast<unsigned long long *>(smem);
 	SchedSmem *fs = reinterpret_cast<SchedSmem *>(rx + F);
 	uint32_t *ts = reinterpret_cast<uint32_t *>(fs + F);
 	uint32_t *id = ts + F + 1;
 	__shared__ uint32_t s_G;
-	__shared__ uint32_t s_sj;  // (streaming) the workers sweep after this step; ~0u: not yet
+	__shared__ uint32_t s_sj;  // (streaming) the launch ends after this step; ~0u: not yet
 	const uint32_t lane = threadIdx.x & 31;
 	constexpr uint32_t TV = 32;  // window vertices per tile: one warp's worth
 
-	uint32_t step0 = 0;  // (streaming) a worker enters the step loop at a later step
-	if constexpr(STREAM)
+	if(threadIdx.x == 0)
 	{
-		if(threadIdx.x == 0) s_sj = ~0u;
-		if(blockIdx.x >= a.ctas)
-		{
-			stream_worker(a, blockIdx.x - a.ctas);
-			const unsigned long long h = stream_join(a.snap, a.bar, F);
-			if(!h) return;
-			step0 = (uint32_t) h;
-			if(threadIdx.x == 0)
-			{
-				s_G = (uint32_t) (h >> 32);
-				s_sj = step0 - 1;
-			}
-		}
+		s_G = 0;
+		if(STREAM) s_sj = ~0u;
 	}
+	__syncthreads();
 	bool waiting = false;  // (streaming) a streamed field waits for its rings
-	if(!step0)
+	for(uint32_t base = 0; base < F; base += NT)
 	{
-		if(threadIdx.x == 0) s_G = 0;
-		__syncthreads();
-		for(uint32_t base = 0; base < F; base += NT)
+		const uint32_t f = base + threadIdx.x;
+		const bool on = f < F && a.state[f].big && a.state[f].live;
+		uint32_t tot;
+		const uint32_t ex = block_exclusive_scan<NT>(on ? 1u : 0u, &tot);
+		if(on)
 		{
-			const uint32_t f = base + threadIdx.x;
-			const bool on = f < F && a.state[f].big && a.state[f].live;
-			uint32_t tot;
-			const uint32_t ex = block_exclusive_scan<NT>(on ? 1u : 0u, &tot);
-			if(on)
-			{
-				const FieldState &g = a.state[f];
-				const uint32_t q = s_G + ex;
-				SchedSmem &x = fs[q];
-				id[q] = f;
-				x.live = 1;
-				x.i = g.i;
-				x.j = g.j;
-				x.d = g.d;
-				x.iter = g.iter;
-				x.n_iter = g.n_iter;
-				x.max_iter = g.max_iter;
-				x.nl = g.n_limits;
-				x.win_s = g.win_s;
-				x.win_e = g.win_e;
-				x.chk_e = g.chk_e;
-				if constexpr(STREAM)
-					if(a.fields[f].stream)
-					{
-						x.live = (a.fields[f].stream << 24) | (1u << 8);  // waits to open its first window
-						waiting = true;
-					}
-				rx[q] = g.relax;
-			}
-			__syncthreads();
-			if(threadIdx.x == 0) s_G += tot;
-			__syncthreads();
+			const FieldState &g = a.state[f];
+			const uint32_t q = s_G + ex;
+			SchedSmem &x = fs[q];
+			id[q] = f;
+			x.live = 1;
+			x.i = g.i;
+			x.j = g.j;
+			x.d = g.d;
+			x.iter = g.iter;
+			x.n_iter = g.n_iter;
+			x.max_iter = g.max_iter;
+			x.nl = g.n_limits;
+			x.win_s = g.win_s;
+			x.win_e = g.win_e;
+			x.chk_e = g.chk_e;
+			if constexpr(STREAM)
+				if(a.fields[f].stream)
+				{
+					x.live = (a.fields[f].stream << 24) | (1u << 8);  // waits to open its first window
+					waiting = true;
+				}
+			rx[q] = g.relax;
 		}
+		__syncthreads();
+		if(threadIdx.x == 0) s_G += tot;
+		__syncthreads();
 	}
 	// (streaming) some streamed field waits for rings: set at the boundary of
 	// step s in [(s + 1) & 1], read at the top of step s + 1 (kept in shared
@@ -1558,28 +1463,24 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 	grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
 	for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
 
-	// (a worker that joined starts after s_sj: read from shared memory here, as
-	// a register held from the branch above raised the sweep loop's spills)
-	for(uint32_t step = STREAM && blockIdx.x >= a.ctas ? s_sj + 1 : 0u;; step++)
+	for(uint32_t step = 0;; step++)
 	{
 		const uint32_t total = ts[G];
-		// the sweeping CTAs: the whole launch, or (streaming) all but the workers
-		// until they join
-		const uint32_t C = STREAM && step <= s_sj ? a.ctas : gridDim.x;
-		if(blockIdx.x == 0 && threadIdx.x == 0 && a.steps && step < a.steps_cap)
+		if(blockIdx.x == 0 && threadIdx.x == 0 && a.steps)
 		{
-			uint32_t live = 0;
-			for(uint32_t q = 0; q < G; q++) live += fs[q].live & 1u;
-			a.steps[2 * step] = global_ns();
-			a.steps[2 * step + 1] = ((unsigned long long) total << 32) | live;
+			// a launch resuming after a streaming launch continues its trace
+			const uint32_t k = step + (a.prev ? a.prev[3] : 0u);
+			if(k < a.steps_cap)
+			{
+				uint32_t live = 0;
+				for(uint32_t q = 0; q < G; q++) live += fs[q].live & 1u;
+				a.steps[2 * k] = global_ns();
+				a.steps[2 * k + 1] = ((unsigned long long) total << 32) | live;
+			}
 		}
 		if(!total && (!STREAM || !s_wait[step & 1]))
 		{
-			if(blockIdx.x == 0 && threadIdx.x == 0)
-			{
-				a.bar[3] = step;
-				if(STREAM && s_sj == ~0u) st_release(a.snap + SNAP_HAND, HAND_END);
-			}
+			if(blockIdx.x == 0 && threadIdx.x == 0) a.bar[3] = step;
 			const uint32_t w = __reduce_add_sync(0xffffffffu, n_skip);
 			if(lane == 0 && w) atomicAdd(reinterpret_cast<unsigned long long *>(a.bar + 4), (unsigned long long) w);
 			break;
@@ -1589,9 +1490,8 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			{
 				// s_wait[(step - 1) & 1] was read at the top of the previous step
 				s_wait[(step + 1) & 1] = 0;
-				// every worker done at the previous step's snapshot: the workers sweep
-				// after this step (C of this step is a.ctas either way, so the other
-				// threads' unordered reads of s_sj agree)
+				// every worker done at the previous step's snapshot: the launch ends
+				// after this step's boundary (read there, after the barrier)
 				if(s_sj == ~0u && a.workers && ldcg(a.snap + SNAP_DONE + ((step - 1) & 1)) == a.workers) s_sj = step;
 				// steps without tiles only while streamed fields wait for rings: bounded
 				if(total) s_idle = 0;
@@ -1645,9 +1545,7 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			// one atomic per warp that saw a failure, no block barrier per tile
 			if(__any_sync(0xffffffffu, bad) && lane == 0) atomicOr(flags + f, 1u);
 		}
-		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom, STREAM ? a.ctas : gridDim.x,
-		                  STREAM ? &s_sj : nullptr, gridDim.x - a.ctas))
-			return;
+		if(!count_barrier(a.bar, step, a.spin_limit, a.phantom, C)) return;
 		// every CTA advances its own copy of every schedule
 		for(uint32_t q = threadIdx.x; q < G; q += NT)
 		{
@@ -1706,7 +1604,17 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 		}
 		__syncthreads();
 		if constexpr(STREAM)
-			if(s_sj == step && blockIdx.x == 0) stream_handover(a.snap, F, G, step);
+			if(s_sj == step)
+			{
+				// every streamed field's toplesets are done, and every streamed field
+				// is a plain field from this boundary on: the schedules go back to
+				// the FieldState (below), and the plain kernel's launch that follows
+				// sweeps the rest
+				if(blockIdx.x == 0 && threadIdx.x == 0) a.bar[3] = step + 1;
+				const uint32_t w = __reduce_add_sync(0xffffffffu, n_skip);
+				if(lane == 0 && w) atomicAdd(reinterpret_cast<unsigned long long *>(a.bar + 4), (unsigned long long) w);
+				break;
+			}
 		grid_plan<TV, STREAM>(fs, ts, G, &s_tile);
 		for(uint32_t q = threadIdx.x; q < G; q += NT) prefetch_limits<STREAM>(a.fields[id[q]], fs[q]);
 	}
@@ -1720,8 +1628,17 @@ __global__ void __launch_bounds__(NT, GP_GRID_MINB) ptp_kernel(GridArgs a)
 			g.d = x.d;
 			g.iter = x.iter;
 			g.n_iter = x.n_iter;
-			g.live = 0;
 			g.relax = rx[q];
+			// (streaming: the launch that resumes reads the open windows)
+			g.live = STREAM ? x.live & 1u : 0u;
+			if constexpr(STREAM)
+			{
+				g.max_iter = x.max_iter;
+				g.n_limits = x.nl;
+				g.win_s = x.win_s;
+				g.win_e = x.win_e;
+				g.chk_e = x.chk_e;
+			}
 		}
 }
 
@@ -2545,17 +2462,27 @@ cudaError_t launch_ptp(FieldDev *fields, FieldState *state, uint32_t n_fields, u
 	if(e != cudaSuccess) return e;
 	const uint32_t w = n_stream ? workers : 0u;
 	GridArgs a{fields,  state, n_fields, notok, bar,      steps, steps_cap, ctl, spin_limit ? spin_limit : SPIN_LIMIT,
-	           phantom, sids,  n_stream, w,     ctas - w, sprog, snap};
+	           phantom, sids,  n_stream, w,     ctas - w, sprog, snap,     nullptr};
 	void *args[] = {&a};
-	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters, n_stream != 0), dim3(ctas), dim3(NT), args,
+	e = cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters, n_stream != 0), dim3(ctas), dim3(NT), args,
+	                                grid_smem_bytes(n_fields), s);
+	if(e != cudaSuccess || !n_stream) return e;
+	// the streaming launch ends once every streamed field's toplesets are done;
+	// the plain kernel sweeps the rest from the FieldState, on the second half
+	// of the barrier line and with fresh ring-test flags
+	e = cudaMemsetAsync(notok, 0, 3 * sizeof(uint32_t) * n_fields, s);
+	if(e != cudaSuccess) return e;
+	GridArgs b{fields,  state, n_fields, notok,   bar + BAR_RESUME, steps,   steps_cap, ctl, a.spin_limit,
+	           phantom, sids,  0u,       0u,      ctas,             nullptr, nullptr,   bar};
+	void *bargs[] = {&b};
+	return cudaLaunchCooperativeKernel(ptp_kernel_ptr(f64, clusters, false), dim3(ctas), dim3(NT), bargs,
 	                                   grid_smem_bytes(n_fields), s);
 }
 
-// 64-bit words of GridArgs::snap for n_fields fields (snapshots, hand-over
-// words and the handed-over schedules)
-size_t ptp_snap_words(uint32_t n_fields)
+// 64-bit words of GridArgs::snap (progress snapshots and the done counts)
+size_t ptp_snap_words(uint32_t)
 {
-	return SNAP_STATE + ((size_t) (SCHED_WORDS + 3) * n_fields + 1) / 2;
+	return SNAP_WORDS;
 }
 
 static const void *ptp_local_ptr(bool f64, bool clusters)

@@ -105,9 +105,10 @@ def test_streaming_off_where_it_does_not_apply(gpu_ctx):
 def test_default_streams_large_fields_of_larger_calls(gpu_ctx):
     """stream_min 0 (the default) streams the fields on meshes of at least
     2^18 vertices once a call has more than 8 fields, and never in smaller
-    calls, whose large fields build their toplesets with the whole GPU; the
-    streamed launch's workers join the sweeps once their toplesets are done,
-    and every output equals the unstreamed call's."""
+    calls, whose large fields build their toplesets with the whole GPU; once
+    the streamed fields' toplesets are done the streaming launch ends and a
+    launch of the plain kernel sweeps the rest, and every output equals the
+    unstreamed call's."""
     from gproshan_gb300 import _capi, meshgen
     big = _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(520, 1))
     big2 = _capi.DeviceMesh(gpu_ctx, *meshgen.torus(200, 1400, seed=2))
@@ -127,9 +128,10 @@ def test_default_streams_large_fields_of_larger_calls(gpu_ctx):
 def test_streaming_launch_gives_up_cleanly(gpu_ctx):
     """A grid barrier that cannot complete (test hook: one arrival more than
     the launch has) with streamed fields in the launch: the sweeping CTAs give
-    up after their poll limit, the workers leave their BFS and their wait for
-    the hand-over on the abort flag, the call reports GP_ERR_DEVICE_TIMEOUT,
-    and the context then gives the unstreamed call's bits."""
+    up after their poll limit, the workers leave their BFS on the abort flag,
+    the launch that would resume the sweeps sees it and returns, the call
+    reports GP_ERR_DEVICE_TIMEOUT, and the context then gives the unstreamed
+    call's bits."""
     from gproshan_gb300 import _capi, meshgen
     big = _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(520, 1))
     _, dms = _meshes(gpu_ctx)
