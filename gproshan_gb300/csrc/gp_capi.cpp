@@ -300,6 +300,16 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	while(!sids.empty() && (sids.size() + STREAM_PER_WORKER - 1) / STREAM_PER_WORKER > ctas / 4) sids.pop_back();
 	const uint32_t n_stream = (uint32_t) sids.size();
 	const uint32_t workers = (n_stream + STREAM_PER_WORKER - 1) / STREAM_PER_WORKER;
+	if(n_stream > workers)
+	{
+		// worker w builds the fields at positions w, w + workers: pair the
+		// largest with the smallest, so that the largest fields' BFS (the
+		// longest) shares its worker with the shortest (batch grid phase
+		// 80.4 -> 79.9 ms against pairing by size order)
+		std::vector<uint32_t> o(sids.begin(), sids.begin() + workers);
+		for(uint32_t k = n_stream; k-- > workers;) o.push_back(sids[k]);
+		sids.swap(o);
+	}
 
 	// ---- checks and layout -------------------------------------------------
 	std::vector<uint32_t> base(F + 1), vbase(F + 1), fbase(F + 1), sbase(F + 1);
