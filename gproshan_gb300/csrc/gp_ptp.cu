@@ -1122,9 +1122,10 @@ __device__ __forceinline__ void grid_plan(const SchedSmem *fs, uint32_t *ts, uin
 // through L1, which other SMs' writes do not update, so no 128-byte line a
 // sweep touches may still change (field bases are aligned to STREAM_ALIGN
 // slots for the same reason).  The readiness every sweeping CTA acts on is a
-// snapshot CTA 0 takes before it arrives at the step's barrier, so all copies
-// of the schedules take the same decisions; a field that waits just skips
-// steps.  The sweeps are the same sweeps in the same order as without
+// snapshot CTA 0 takes at the start of the step (before its arrival at the
+// step's barrier), so all copies of the schedules take the same decisions; a
+// field that waits just skips steps.  The sweeps are the same sweeps in the
+// same order as without
 // streaming, so the results are bit-identical.  Once every worker is done
 // (the first boundary whose snapshot counts them all), the launch writes every
 // schedule back to its FieldState and ends; a launch of the plain lockstep
