@@ -125,6 +125,35 @@ def test_default_streams_large_fields_of_larger_calls(gpu_ctx):
     assert gpu_ctx.call_stats().fields_streamed == 0
 
 
+def test_streamed_fields_with_normalize(gpu_ctx):
+    """normalize in a call with streamed fields (the maximum reduced in the
+    output gather, after both grid launches): the same bits as the unstreamed
+    normalized call, and each field is its plain output over its largest
+    finite distance."""
+    from gproshan_gb300 import _capi, meshgen
+    big = _capi.DeviceMesh(gpu_ctx, *meshgen.height_field(520, 1))
+    _, dms = _meshes(gpu_ctx)
+    ms = [big, dms[0], big] + dms[1:8]
+    srcs = [[3], [0], [200000]] + [[1]] * 7
+    plain, _, _ = _run(gpu_ctx, ms, srcs, NEVER)
+    L = _capi.lib()
+    got = {}
+    for smin in (1 << 18, NEVER):
+        outs = [np.empty(m.n_vertices, np.float32) for m in ms]
+        fields, keep = _capi._fields(ms, srcs, outs)
+        o = _capi.make_opts(_capi.GP_F32, normalize=True, grid_kernel=_capi.GP_GRID_LOCKSTEP, stream_min=smin)
+        sec = _capi.C.c_double()
+        gpu_ctx.check(L.gp_ptp_batch(gpu_ctx.handle, fields, len(ms), _capi.C.byref(o), _capi.GP_F32, 0,
+                                     _capi.C.byref(sec)), "batch")
+        got[smin] = (outs, gpu_ctx.call_stats().fields_streamed)
+    assert got[1 << 18][1] == 2 and got[NEVER][1] == 0
+    for a, b, p in zip(got[1 << 18][0], got[NEVER][0], plain):
+        assert np.array_equal(a, b)
+        ref = p.copy()
+        ref /= np.float32(np.max(ref[np.isfinite(ref)]))
+        assert np.array_equal(a, ref)
+
+
 def test_streaming_launch_gives_up_cleanly(gpu_ctx):
     """A grid barrier that cannot complete (test hook: one arrival more than
     the launch has) with streamed fields in the launch: the sweeping CTAs give
