@@ -1142,15 +1142,25 @@ constexpr uint32_t SNAP_DONE = 2 * STREAM_MAX, SNAP_WORKERS = SNAP_DONE + 2;
 constexpr uint32_t SNAP_WORDS = SNAP_DONE + 4, SNAP_CTL_WORDS = 4;
 
 // Ring positions [k0, k1) of streamed field F: the FP32 sweeps' padded fan
-// rows, positions and initial distances, as fill_kernel writes them.
-__device__ __forceinline__ void stream_renumber(const FieldDev &F, uint32_t k0, uint32_t k1)
+// rows, positions and initial distances, as fill_kernel writes them.  The
+// first chunk's vertex and mesh rows (position k0 + threadIdx.x) come from
+// the caller, which loaded them for the same positions in the level's
+// discover pass: one dependent L2 trip fewer per ring.
+__device__ __forceinline__ void stream_renumber(const FieldDev &F, uint32_t k0, uint32_t k1, uint32_t v0,
+                                                uint4 ra0, uint4 rb0)
 {
 	float2 *D0 = static_cast<float2 *>(F.D[0]);
 	float2 *D1 = static_cast<float2 *>(F.D[1]);
 	for(uint32_t k = k0 + threadIdx.x; k < k1; k += NT)
 	{
-		const uint32_t v = ldcg(F.sorted + k);
-		const uint4 ra = __ldg(F.m.fan8 + 2 * (size_t) v), rb = __ldg(F.m.fan8 + 2 * (size_t) v + 1);
+		uint32_t v = v0;
+		uint4 ra = ra0, rb = rb0;
+		if(k >= k0 + NT)
+		{
+			v = ldcg(F.sorted + k);
+			ra = __ldg(F.m.fan8 + 2 * (size_t) v);
+			rb = __ldg(F.m.fan8 + 2 * (size_t) v + 1);
+		}
 		uint32_t r[8], n = 0;
 #pragma unroll
 		for(uint32_t q = 0; q < 8; q++)
@@ -1301,7 +1311,7 @@ __device__ __noinline__ void stream_worker(const GridArgs &a, uint32_t w)
 			}
 			__syncthreads();
 			// ring `level` = [s, e): all its neighbours have their new ids now
-			stream_renumber(F, s, e);
+			stream_renumber(F, s, e, v0, ra, rb);
 			__syncthreads();
 			if(threadIdx.x == 0)
 			{
