@@ -296,18 +296,35 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	}
 	const int maxc = stage == Stage::ptp ? ptp_max_ctas(ctx->device, f64, clusters, F) : 0;
 	const uint32_t ctas = o.ctas ? std::min<uint32_t>(o.ctas, (uint32_t) maxc) : (uint32_t) maxc;
-	// workers take at most a quarter of the launch's CTAs
-	while(!sids.empty() && (sids.size() + STREAM_PER_WORKER - 1) / STREAM_PER_WORKER > ctas / 4) sids.pop_back();
-	const uint32_t n_stream = (uint32_t) sids.size();
-	const uint32_t workers = (n_stream + STREAM_PER_WORKER - 1) / STREAM_PER_WORKER;
-	if(n_stream > workers)
+	// Workers: the fields of at least 3/4 of the largest's vertices (the
+	// longest BFS) get a worker each, the others two per worker, the largest
+	// of them with the smallest.  Worker w builds the fields at positions w and
+	// w + workers (gp_ptp.cu: stream_worker), so the order is: the larger
+	// halves of the pairs, the solo fields, the smaller halves reversed.
+	// (Benchmark batch, grid phase: pairs by size order 80.4 ms, largest with
+	// smallest 79.9; the same box, pairs only 79.78 against the 1M-vertex
+	// fields solo 79.62.)  Workers take at most a quarter of the launch's CTAs.
+	static_assert(STREAM_PER_WORKER == 2, "the order below pairs fields two per worker");
+	uint32_t workers = 0;
+	for(;;)
 	{
-		// worker w builds the fields at positions w, w + workers: pair the
-		// largest with the smallest, so that the largest fields' BFS (the
-		// longest) shares its worker with the shortest (batch grid phase
-		// 80.4 -> 79.9 ms against pairing by size order)
-		std::vector<uint32_t> o(sids.begin(), sids.begin() + workers);
-		for(uint32_t k = n_stream; k-- > workers;) o.push_back(sids[k]);
+		const uint32_t n = (uint32_t) sids.size();
+		uint32_t solo = 0;
+		while(solo < n && 4ull * reqs[sids[solo]].mesh->nv >= 3ull * reqs[sids[0]].mesh->nv) solo++;
+		workers = solo + (n - solo + STREAM_PER_WORKER - 1) / STREAM_PER_WORKER;
+		if(workers <= ctas / 4 || sids.empty()) break;
+		sids.pop_back();
+	}
+	const uint32_t n_stream = (uint32_t) sids.size();
+	if(n_stream)
+	{
+		uint32_t solo = 0;
+		while(solo < n_stream && 4ull * reqs[sids[solo]].mesh->nv >= 3ull * reqs[sids[0]].mesh->nv) solo++;
+		const uint32_t rest = n_stream - solo, big = (rest + 1) / 2;
+		std::vector<uint32_t> o;
+		o.insert(o.end(), sids.begin() + solo, sids.begin() + solo + big);  // positions [0, big)
+		o.insert(o.end(), sids.begin(), sids.begin() + solo);                // [big, workers)
+		for(uint32_t k = n_stream; k-- > solo + big;) o.push_back(sids[k]);   // [workers, n)
 		sids.swap(o);
 	}
 
