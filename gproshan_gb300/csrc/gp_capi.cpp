@@ -419,7 +419,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	const size_t o_pbig = cv.add<uint32_t>(F), o_cost = cv.add<float>(F), o_perm = cv.add<uint32_t>(F);
 	const size_t o_qf = cv.add<QField>(F), o_qcur = cv.add<QLine>((size_t) F * QUEUE_STRIPES);
 	const size_t o_qdone = cv.add<QLine>((size_t) F * QUEUE_STRIPES), o_qsd = cv.add<QLine>(F);
-	const size_t o_qctl = cv.add<QCtl>(1), o_model = cv.add<float>(MLP_NPARAM);
+	const size_t o_qctl = cv.add<QCtl>(1), o_model = cv.add<float>(MLP_NPARAM), o_border = cv.add<uint32_t>(F);
 	std::vector<uint32_t> wide;
 	if(!given_tops && wide_bfs)
 		for(uint32_t f = 0; f < F; f++)
@@ -522,9 +522,21 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 				hf[f].clusters_in = reinterpret_cast<uint32_t *>(P(o_cin)) + vbase[f];
 
 	// ---- uploads -------------------------------------------------------------
+	// the one-CTA BFS takes the fields largest first, so that the longest BFS
+	// do not start in a second wave of CTAs (streamed fields, skipped there, last)
+	std::vector<uint32_t> border(F);
+	for(uint32_t f = 0; f < F; f++) border[f] = f;
+	std::stable_sort(border.begin(), border.end(), [&](uint32_t x, uint32_t y) {
+		const uint64_t kx = hf[x].stream ? 0u : reqs[x].mesh->nv, ky = hf[y].stream ? 0u : reqs[y].mesh->nv;
+		return kx > ky;
+	});
 	cudaStream_t s = ctx->stream;
-	size_t pin_need = sizeof(FieldDev) * F + sizeof(FieldState) * F + 8 * (F + 1) + 4 * (size_t) stot + 64;
-	if(given_tops) pin_need += 4 * ((size_t) reqs[0].nl + reqs[0].limits[reqs[0].nl - 1]) + 64;
+	// every staged copy below, each rounded up to 16 bytes
+	const auto a16 = [](size_t b) { return align_up(b, 16); };
+	size_t pin_need = a16(sizeof(FieldDev) * F) + a16(sizeof(FieldState) * F) + 2 * a16(4 * (size_t) (F + 1)) +
+	                  a16(4 * wide.size()) + a16(4 * (size_t) n_stream) + a16(4 * (size_t) F);
+	pin_need += fps ? a16(4 * (size_t) fps->n_init) + a16(sizeof(FpsDev)) : a16(4 * (size_t) stot);
+	if(given_tops) pin_need += a16(4 * (size_t) reqs[0].nl) + a16(4 * (size_t) reqs[0].limits[reqs[0].nl - 1]);
 	st = ensure_pin(ctx, pin_need);
 	if(st != GP_OK) return st;
 	GP_CUDA(ctx, cudaStreamSynchronize(s));  // the staging buffer may still feed a previous call
@@ -542,6 +554,7 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 	GP_CUDA(ctx, stage_copy(o_vbase, vbase.data(), 4 * (F + 1)));
 	if(!wide.empty()) GP_CUDA(ctx, stage_copy(o_wide, wide.data(), 4 * wide.size()));
 	if(n_stream) GP_CUDA(ctx, stage_copy(o_sids, sids.data(), 4 * (size_t) n_stream));
+	GP_CUDA(ctx, stage_copy(o_border, border.data(), 4 * (size_t) F));
 	if(fps)
 	{
 		// the seeds; the field's source count starts at n_init and grows on the device
@@ -614,7 +627,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			                                   reinterpret_cast<uint32_t *>(P(o_wtot)), (uint32_t) ctx->bfs_wide_ctas, s));
 			cs.launches += 1;
 		}
-		GP_CUDA(ctx, launch_toplesets(dF, dS, F, &dSync->count, (uint32_t) ctx->bfs_ctas, s));
+		GP_CUDA(ctx, launch_toplesets(dF, dS, F, &dSync->count, (uint32_t) ctx->bfs_ctas,
+		                              reinterpret_cast<const uint32_t *>(P(o_border)), s));
 		cs.launches += (vtot ? 1 : 0) + 2;
 	}
 	GP_CUDA(ctx, record(ctx->ph[1]));

@@ -196,9 +196,10 @@ size_t scan_tmp_words(size_t n);
 cudaError_t launch_scan_u32(const uint32_t *in, uint32_t *out, size_t n, uint32_t *tmp, cudaStream_t s);
 cudaError_t launch_max_u32(const uint32_t *in, size_t n, uint32_t *out, cudaStream_t s);
 
-// gp_toplesets.cu: BFS of all fields; fills ring/sorted/limits and state[f].n_limits.
+// gp_toplesets.cu: BFS of all fields (taken in `order`, or by index if null);
+// fills ring/sorted/limits and state[f].n_limits.
 cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
-                             uint32_t ctas, cudaStream_t s);
+                             uint32_t ctas, const uint32_t *order, cudaStream_t s);
 int toplesets_max_ctas(int device);
 size_t che_build_scratch_bytes(uint32_t nv, uint32_t nhe);
 gp_status off_parse(const char *path, std::vector<double> &xyz, std::vector<uint32_t> &tri, std::string &err);

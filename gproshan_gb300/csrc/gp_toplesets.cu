@@ -40,7 +40,7 @@ constexpr uint32_t KB = GP_KB;
 constexpr uint32_t SF = BT * KB;
 
 __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState *state, uint32_t n_fields,
-                                                 uint32_t *queue)
+                                                 uint32_t *queue, const uint32_t *order)
 {
 	__shared__ uint32_t s_f;
 	__shared__ uint32_t sf[2][SF];  // frontier copies: current and next level
@@ -48,9 +48,10 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 	{
 		if(threadIdx.x == 0) s_f = atomicAdd(queue, 1u);
 		__syncthreads();
-		const uint32_t f = s_f;
+		const uint32_t ticket = s_f;
 		__syncthreads();
-		if(f >= n_fields) return;
+		if(ticket >= n_fields) return;
+		const uint32_t f = order ? order[ticket] : ticket;
 		const FieldDev &F = fields[f];
 		if(!state[f].bfs_live || F.stream) continue;  // no sources, a source out of range, or streamed
 
@@ -439,14 +440,15 @@ cudaError_t launch_toplesets_wide(FieldDev *fields, FieldState *state, const uin
 	return cudaLaunchCooperativeKernel((const void *) bfs_grid_kernel, dim3(ctas), dim3(BG), args, 0, s);
 }
 
-// queue: one word, zeroed here (the field ticket)
+// queue: one word, zeroed here (the field ticket); order: the fields in the
+// order the CTAs take them (null: by index)
 cudaError_t launch_toplesets(FieldDev *fields, FieldState *state, uint32_t n_fields, uint32_t *queue,
-                             uint32_t ctas, cudaStream_t s)
+                             uint32_t ctas, const uint32_t *order, cudaStream_t s)
 {
 	cudaError_t e = cudaMemsetAsync(queue, 0, sizeof(uint32_t), s);
 	if(e != cudaSuccess) return e;
 	ctas = std::max<uint32_t>(1, std::min<uint32_t>(ctas, n_fields));
-	bfs_kernel<<<ctas, BT, 0, s>>>(fields, state, n_fields, queue);
+	bfs_kernel<<<ctas, BT, 0, s>>>(fields, state, n_fields, queue, order);
 	return cudaGetLastError();
 }
 
@@ -578,7 +580,7 @@ extern "C" gp_status gp_toplesets_noalloc(const gp_mesh *mesh, const uint32_t *s
 	bfs_clear_kernel<<<(unsigned) std::min<uint32_t>((m->nv + 255) / 256, 152 * 16), 256, 0, s>>>(&h->f, h->vbase, 1,
 	                                                                                              m->nv);
 	bfs_seed_kernel<<<1, 32, 0, s>>>(&h->f, &h->st, 1);
-	bfs_kernel<<<1, BT, 0, s>>>(&h->f, &h->st, 1, &h->queue);
+	bfs_kernel<<<1, BT, 0, s>>>(&h->f, &h->st, 1, &h->queue, nullptr);
 	noalloc_finish_kernel<<<1, 32, 0, s>>>(n_limits);
 	return cudaGetLastError() == cudaSuccess ? GP_OK : GP_ERR_CUDA;
 }
