@@ -1993,6 +1993,9 @@ struct CatArgs {
 	uint32_t *cnt;         // total (+1) counts, then global fan offsets after the scan
 	unsigned long long *amax = nullptr;  // gather only: null, or max |out| (bits) of the call, atomicMax'ed
 	bool nmax = false;                   // gather only: reduce each field's largest finite output into state.nmax
+	// renumbering: write the CSR fan offsets (FP64, or FP32 rows longer than
+	// a fan8 row can hold); false: cnt is not computed and off not written
+	bool csr = true;
 };
 
 __global__ void inv_clear_kernel(CatArgs c)
@@ -2058,8 +2061,8 @@ __global__ void fill_kernel(CatArgs c)
 			const uint32_t v = F.sorted[k];
 			const uint32_t o0f = F.m.fan_off[v];
 			const uint32_t o0 = o0f & FAN_MASK, o1 = F.m.fan_off[v + 1] & FAN_MASK;
-			const uint32_t dst = c.cnt[g];
-			F.off[k] = dst | (o0f & FAN_CLOSED);
+			const uint32_t dst = c.csr ? c.cnt[g] : 0u;
+			if(c.csr) F.off[k] = dst | (o0f & FAN_CLOSED);
 			{
 				uint32_t r[8];
 				const uint32_t n = o1 - o0;
@@ -2136,7 +2139,7 @@ __global__ void fill_kernel(CatArgs c)
 		}
 		else if(k == nr)
 		{
-			F.off[k] = c.cnt[g];
+			if(c.csr) F.off[k] = c.cnt[g];
 			F.fan8[2 * (size_t) k] = make_uint4(0u, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);  // count 0
 			F.fan8[2 * (size_t) k + 1] = make_uint4(FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY, FAN8_EMPTY);
 			F.P[k] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -2312,17 +2315,24 @@ unsigned grid_for(uint64_t n)
 // launchers
 // ---------------------------------------------------------------------------
 
+// csr: the FP32 sweeps read the CSR fan only for rows of more than a fan8
+// row's entries, so a call whose meshes have none skips the counts, their
+// scan and the offsets (csr false); FP64 always writes them
 cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
                                   uint32_t total, uint32_t *cnt, uint32_t *scan_tmp, bool f64, bool clusters,
-                                  cudaStream_t s)
+                                  bool csr, cudaStream_t s)
 {
 	CatArgs c{fields, state, base, n_fields, total, cnt};
+	c.csr = csr || f64;
 	const unsigned nb = grid_for(total);
 	inv_clear_kernel<<<nb, 256, 0, s>>>(c);
 	inv_set_kernel<<<nb, 256, 0, s>>>(c);
-	count_kernel<<<nb, 256, 0, s>>>(c);
-	cudaError_t e = launch_scan_u32(cnt, cnt, total, scan_tmp, s);
-	if(e != cudaSuccess) return e;
+	if(c.csr)
+	{
+		count_kernel<<<nb, 256, 0, s>>>(c);
+		const cudaError_t e = launch_scan_u32(cnt, cnt, total, scan_tmp, s);
+		if(e != cudaSuccess) return e;
+	}
 	if(f64)
 	{
 		if(clusters) fill_kernel<double, true><<<nb, 256, 0, s>>>(c);
