@@ -25,7 +25,7 @@ cudaError_t launch_bfs_setup(FieldDev *fields, FieldState *state, const uint32_t
                              uint32_t total_vertices, cudaStream_t s);
 cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
                                   uint32_t total, uint32_t *cnt, uint32_t *scan_tmp, bool f64, bool clusters,
-                                  bool csr, cudaStream_t s);
+                                  bool csr, bool inv_ready, cudaStream_t s);
 cudaError_t launch_gather_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
                                 uint32_t total, bool f64, bool clusters, cudaStream_t s, unsigned long long *amax = nullptr, bool nmax = false);
 cudaError_t launch_normalize_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
@@ -644,8 +644,8 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 		// the CSR fan only where a row can outgrow a fan8 row (FP64 always)
 		const bool csr = f64 || std::any_of(reqs, reqs + F, [](const Req &r) { return r.mesh->dev.max_fan > 7; });
 		GP_CUDA(ctx, launch_renumber_batch(dF, dS, dBase, F, (uint32_t) tot, reinterpret_cast<uint32_t *>(P(o_cnt)),
-		                                   reinterpret_cast<uint32_t *>(P(o_scan)), f64, clusters, csr, s));
-		cs.launches += csr ? 4 + scan_launches(tot) : 3;
+		                                   reinterpret_cast<uint32_t *>(P(o_scan)), f64, clusters, csr, !given_tops, s));
+		cs.launches += (csr ? 2 + scan_launches(tot) : 1) + (given_tops ? 2 : 0);
 		GP_CUDA(ctx, record(ctx->ph[2]));
 		// FP64 fields leave the one-CTA launch early: GB300's FP64 pipe retires
 		// ~2 FMAs per clock per SM, so one CTA is throughput-bound on one SM

@@ -2317,16 +2317,21 @@ unsigned grid_for(uint64_t n)
 
 // csr: the FP32 sweeps read the CSR fan only for rows of more than a fan8
 // row's entries, so a call whose meshes have none skips the counts, their
-// scan and the offsets (csr false); FP64 always writes them
+// scan and the offsets (csr false); FP64 always writes them.  inv_ready: the
+// GPU toplesets already wrote inv (positions + 1, 0 for unreached vertices);
+// host-given toplesets need it built here.
 cudaError_t launch_renumber_batch(FieldDev *fields, FieldState *state, const uint32_t *base, uint32_t n_fields,
                                   uint32_t total, uint32_t *cnt, uint32_t *scan_tmp, bool f64, bool clusters,
-                                  bool csr, cudaStream_t s)
+                                  bool csr, bool inv_ready, cudaStream_t s)
 {
 	CatArgs c{fields, state, base, n_fields, total, cnt};
 	c.csr = csr || f64;
 	const unsigned nb = grid_for(total);
-	inv_clear_kernel<<<nb, 256, 0, s>>>(c);
-	inv_set_kernel<<<nb, 256, 0, s>>>(c);
+	if(!inv_ready)
+	{
+		inv_clear_kernel<<<nb, 256, 0, s>>>(c);
+		inv_set_kernel<<<nb, 256, 0, s>>>(c);
+	}
 	if(c.csr)
 	{
 		count_kernel<<<nb, 256, 0, s>>>(c);

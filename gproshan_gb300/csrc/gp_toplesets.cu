@@ -126,6 +126,7 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 							{
 								F.sorted[e + o] = u;
 								F.ring[u] = level + 1;
+								if(F.inv) F.inv[u] = e + o + 1;
 								if(o < SF) sf[cur ^ 1][o] = u;
 								o++;
 							}
@@ -139,6 +140,7 @@ __global__ void __launch_bounds__(BT, 1) bfs_kernel(FieldDev *fields, FieldState
 								const uint32_t u = slot_of(a, b, q);
 								F.sorted[e + o] = u;
 								F.ring[u] = level + 1;
+								if(F.inv) F.inv[u] = e + o + 1;
 								if(o < SF) sf[cur ^ 1][o] = u;
 								o++;
 							}
@@ -220,6 +222,7 @@ __device__ __forceinline__ void emit_owned(const FieldDev &F, uint32_t p, uint32
 	auto put = [&](uint32_t u) {
 		F.sorted[o] = u;
 		F.ring[u] = level + 1;
+		if(F.inv) F.inv[u] = o + 1;
 		uint4 ua, ub;
 		load_row(F, u, ua, ub);
 		discover(F, o, u, ua, ub);
@@ -365,6 +368,7 @@ __global__ void bfs_clear_kernel(FieldDev *fields, const uint32_t *vbase, uint32
 		const uint32_t v = g - vbase[f];
 		fields[f].ring[v] = NIL;
 		fields[f].key[v] = ~0ull;
+		if(fields[f].inv) fields[f].inv[v] = 0;  // position + 1 of v, 0: unreached
 	}
 }
 
@@ -391,6 +395,7 @@ __global__ void bfs_seed_kernel(FieldDev *fields, FieldState *state, uint32_t n_
 		F.sorted[s] = v;
 		F.ring[v] = 0;
 		F.key[v] = 0;  // below every discovery key: a source is never re-discovered
+		if(F.inv) F.inv[v] = s + 1;  // repeated sources: the last occurrence
 	}
 	F.limits[0] = 0;
 	F.limits[1] = F.ns;
