@@ -688,7 +688,9 @@ gp_status run(gp_ctx *ctx, const Req *reqs, uint32_t F, const gp_ptp_opts *opts,
 			GP_CUDA(ctx, launch_normalize_batch(dF, dS, dBase, F, (uint32_t) tot, out_type == GP_F64, s));
 			cs.launches += 1;
 		}
-		cs.launches += 6;
+		// classify, one-CTA sweeps, queue setup + queue kernel, lockstep (and with
+		// streamed fields the plain launch that resumes after it), gather
+		cs.launches += 6 + (n_stream ? 1 : 0);
 	}
 	else
 		for(int k = 2; k < 5; k++) GP_CUDA(ctx, record(ctx->ph[k]));
