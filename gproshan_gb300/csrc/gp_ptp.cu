@@ -2173,16 +2173,28 @@ __global__ void gather_kernel(CatArgs c)
 		const FieldState &st = c.state[f];
 		const uint32_t iv = F.inv[v];
 		const uint32_t k = iv ? iv - 1 : st.nr;
-		double x;
+		// y: the value written (as a double, for the maxima below)
+		double y;
 		if constexpr(sizeof(T) == 4)
 		{
 			const float2 h = unflag(static_cast<const float2 *>(F.D[st.d])[k]);
-			x = (double) h.x + (double) h.y;
+			if(F.out_f64) static_cast<double *>(F.dist_out)[v] = y = (double) h.x + (double) h.y;
+			else
+			{
+				// the float nearest hi + lo: one float addition (the double sum of a
+				// normalized pair, at most 49 significant bits, is exact, so rounding
+				// it to float gives the same bits); no FP64 work per vertex
+				const float r = __fadd_rn(h.x, h.y);
+				static_cast<float *>(F.dist_out)[v] = r;
+				y = r;
+			}
 		}
-		else x = static_cast<const double *>(F.D[st.d])[k];
-		double y;
-		if(F.out_f64) static_cast<double *>(F.dist_out)[v] = y = x;
-		else static_cast<float *>(F.dist_out)[v] = (float) x, y = (double) (float) x;
+		else
+		{
+			const double x = static_cast<const double *>(F.D[st.d])[k];
+			if(F.out_f64) static_cast<double *>(F.dist_out)[v] = y = x;
+			else static_cast<float *>(F.dist_out)[v] = (float) x, y = (double) (float) x;
+		}
 		if(CL && F.clusters_out)
 			F.clusters_out[v] = iv ? F.C[st.d][k] : (F.clusters_in ? F.clusters_in[v] : 0u);
 		// farthest-point sampling: max |out| over the call (the value cublasI?amax
